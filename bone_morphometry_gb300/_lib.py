@@ -1,0 +1,171 @@
+"""ctypes binding of libbm_gb300.so (the C ABI declared in include/bm.h).
+
+The library is loaded from this package's in-tree ``_build/`` directory.  If it
+is missing it is built with nvcc; if that is impossible, or no CUDA device is
+present, calls raise ``BoneMorphometryError`` -- there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+BM_OK = 0
+BM_ERR_ALL_SELECTED = 1
+BM_ERR_DIMS = 2
+BM_ERR_OOM = 3
+BM_ERR_CUDA = 4
+BM_ERR_TIMEOUT = 5
+BM_ERR_INVALID = 6
+BM_ERR_EMPTY = 7
+BM_ERR_ROI_EMPTY = 8
+BM_ERR_NO_BONE = 9
+BM_ERR_NO_MARROW = 10
+BM_ERR_NO_DEVICE = 11
+BM_ERR_SPACING = 12
+BM_ERR_ROI_FULL = 13
+BM_ERR_BUSY = 14
+
+BM_FLAG_QUANTILES = 1
+BM_FLAG_BONEJ_ROI = 2
+
+
+class BoneMorphometryError(RuntimeError):
+    """A non-zero bm_status from the library, with the reference's message text."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+class BmStats(ctypes.Structure):
+    _fields_ = [
+        ("count", ctypes.c_uint64),
+        ("mean", ctypes.c_double),
+        ("standard_deviation", ctypes.c_double),
+        ("maximum", ctypes.c_double),
+        ("median", ctypes.c_double),
+        ("percentile_10", ctypes.c_double),
+        ("percentile_25", ctypes.c_double),
+        ("percentile_75", ctypes.c_double),
+        ("percentile_90", ctypes.c_double),
+        ("interquartile_range", ctypes.c_double),
+        ("coefficient_of_variation", ctypes.c_double),
+        ("sum", ctypes.c_double),
+        ("sum_of_squares", ctypes.c_double),
+    ]
+
+
+# name -> (restype, argtypes); every symbol declared in include/bm.h
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+_i = ctypes.c_int
+_u = ctypes.c_uint
+_d = ctypes.c_double
+_pctx = ctypes.c_void_p
+_u8p = ctypes.c_void_p
+SIGNATURES = {
+    "bm_ctx_create": (_i, [_i, ctypes.POINTER(ctypes.c_void_p)]),
+    "bm_ctx_destroy": (None, [_pctx]),
+    "bm_status_string": (ctypes.c_char_p, [_i]),
+    "bm_last_error": (_sz, [_pctx, ctypes.c_char_p, _sz]),
+    "bm_ctx_trim": (_i, [_pctx]),
+    "bm_edt_sq": (_i, [_pctx, _u8p, _sz, _sz, _sz, _i, _vp]),
+    "bm_local_thickness": (_i, [_pctx, _u8p, _sz, _sz, _sz, _i, _vp, _vp]),
+    "bm_tbth_tbsp": (_i, [_pctx, _u8p, _u8p, _sz, _sz, _sz, _d, _u, ctypes.POINTER(BmStats),
+                          ctypes.POINTER(BmStats), _vp, _vp]),
+    "bm_edt_sq_device": (_i, [_pctx, _u8p, _sz, _sz, _sz, _i, _vp, _vp]),
+    "bm_local_thickness_device": (_i, [_pctx, _u8p, _sz, _sz, _sz, _i, _vp, _vp, _vp]),
+    "bm_tbth_tbsp_device": (_i, [_pctx, _u8p, _u8p, _sz, _sz, _sz, _d, _u, ctypes.POINTER(BmStats),
+                                 ctypes.POINTER(BmStats), _vp, _vp, _vp]),
+    "bm_ctx_launch_count": (ctypes.c_uint64, [_pctx]),
+}
+
+_LIB = None
+_LOCK = threading.Lock()
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load() -> ctypes.CDLL:
+    """Load (building in-tree if absent) libbm_gb300.so and declare its signatures."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = _build.LIB
+        if not os.path.exists(path):
+            try:
+                path = _build.build()
+            except Exception as exc:  # no nvcc / compile error: fail loudly
+                raise BoneMorphometryError(BM_ERR_NO_DEVICE,
+                                           "libbm_gb300.so is missing and could not be built: %s" % exc)
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+        return lib
+
+
+def last_error(ctx) -> str:
+    lib = load()
+    buf = ctypes.create_string_buffer(1024)
+    lib.bm_last_error(ctx, buf, len(buf))
+    return buf.value.decode("utf-8", "replace")
+
+
+def raise_for(status: int, ctx) -> None:
+    if status != BM_OK:
+        msg = last_error(ctx) or load().bm_status_string(status).decode()
+        raise BoneMorphometryError(status, msg)
+
+
+class Context:
+    """Owns one bm_ctx (device, stream, cached buffers and template table)."""
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        h = ctypes.c_void_p()
+        st = lib.bm_ctx_create(int(device), ctypes.byref(h))
+        if st != BM_OK:
+            raise BoneMorphometryError(st, last_error(None) or lib.bm_status_string(st).decode())
+        self.handle = h
+        self.device = device
+        self._lib = lib
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self._lib.bm_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        return int(self._lib.bm_ctx_launch_count(self.handle))
+
+    def call(self, name: str, *args) -> None:
+        st = getattr(self._lib, name)(self.handle, *args)
+        raise_for(st, self.handle)
+
+
+_DEFAULT = {}
+
+
+def default_context(device: int = 0) -> Context:
+    ctx = _DEFAULT.get(device)
+    if ctx is None or ctx.handle is None:
+        ctx = Context(device)
+        _DEFAULT[device] = ctx
+    return ctx

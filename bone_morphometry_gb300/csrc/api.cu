@@ -1,0 +1,492 @@
+// C ABI of libbm_gb300 (include/bm.h): context, buffer cache, the per-phase
+// pipeline and the drop-in entry points for edt.rs / local_thickness.rs /
+// metrics.rs.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "exact_sum.h"
+#include "kernels.h"
+
+using namespace bm;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct CallError {
+  int status;
+};
+
+void set_err(bm_ctx* ctx, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->last_error = buf;
+  else g_create_error = buf;
+}
+
+[[noreturn]] void fail(bm_ctx* ctx, int status, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  ctx->last_error = buf;
+  throw CallError{status};
+}
+
+void check(bm_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  const int st = (e == cudaErrorMemoryAllocation) ? BM_ERR_OOM : BM_ERR_CUDA;
+  cudaGetLastError();  // clear a sticky-free error so the context stays usable
+  fail(ctx, st, "%s: %s", what, cudaGetErrorString(e));
+}
+
+void* ensure(bm_ctx* ctx, Buffer& b, size_t bytes, const char* what) {
+  if (bytes == 0) bytes = 16;
+  if (b.bytes >= bytes) return b.ptr;
+  if (b.ptr) {
+    cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(ctx, BM_ERR_OOM, "device allocation of %zu bytes for %s failed: %s", bytes, what, cudaGetErrorString(e));
+  }
+  b.ptr = p;
+  b.bytes = bytes;
+  return p;
+}
+
+void release(Buffer& b) {
+  if (b.ptr) cudaFree(b.ptr);
+  b.ptr = nullptr;
+  b.bytes = 0;
+}
+
+// volume.rs:12-34 plus the library's own limits (u32 linear ridge index, u32
+// squared distances whose search templates cannot overflow u32).
+Dims check_dims(bm_ctx* ctx, size_t w, size_t h, size_t d) {
+  if (w < 2 || h < 2 || d < 2)
+    fail(ctx, BM_ERR_DIMS, "all dimensions must be at least 2 for 3-D morphometry; got %zux%zux%zu", w, h, d);
+  if (w > 32768 || h > 32768 || d > 32768)
+    fail(ctx, BM_ERR_DIMS, "dimension above 32768 is not supported; got %zux%zux%zu", w, h, d);
+  const unsigned long long n = (unsigned long long)w * h * d;
+  if (n >= 0xFFFFFFFFull)
+    fail(ctx, BM_ERR_DIMS, "volume of %llu voxels exceeds the 2^32-1 voxel limit", n);
+  const unsigned long long r2 =
+      (unsigned long long)(w - 1) * (w - 1) + (unsigned long long)(h - 1) * (h - 1) + (unsigned long long)(d - 1) * (d - 1);
+  if (r2 >= (1ull << 30)) fail(ctx, BM_ERR_DIMS, "largest squared distance %llu exceeds 2^30", r2);
+  return Dims{(int)w, (int)h, (int)d};
+}
+
+const char* phase_name(int phase) { return phase == BM_PHASE_BACKGROUND ? "background" : "foreground"; }
+
+void ensure_lut(bm_ctx* ctx, uint32_t rmax) {
+  if (ctx->lut_max >= rmax && ctx->lut.ptr) return;
+  // grow to at least twice the current size so repeated growth stays amortised
+  uint32_t target = rmax;
+  if (ctx->lut.ptr && target < ctx->lut_max * 2u) target = ctx->lut_max * 2u;
+  if (target < 1024) target = 1024;
+  const size_t bytes = ((size_t)target + 1) * sizeof(uint4);
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(ctx, BM_ERR_OOM, "device allocation of %zu bytes for the template table failed", bytes);
+  }
+  uint32_t lo = 0;
+  if (ctx->lut.ptr) {
+    check(ctx, cudaMemcpyAsync(p, ctx->lut.ptr, ((size_t)ctx->lut_max + 1) * sizeof(uint4), cudaMemcpyDeviceToDevice,
+                               ctx->stream),
+          "template table copy");
+    lo = ctx->lut_max + 1;
+  }
+  check(ctx, launch_lut(static_cast<uint4*>(p), lo, target, ctx->stream, &ctx->launches), "template kernel");
+  check(ctx, cudaStreamSynchronize(ctx->stream), "template kernel");
+  release(ctx->lut);
+  ctx->lut.ptr = p;
+  ctx->lut.bytes = bytes;
+  ctx->lut_max = target;
+}
+
+struct PhaseResult {
+  unsigned long long sites = 0, selected = 0, ridges = 0;
+  uint32_t rmax = 0;
+  StatsAccum acc;
+};
+
+// One phase: EDT (+ local thickness + statistics unless edt_only).
+// d_a / d_b are the device inputs for `mode`; results optionally go to d_edt
+// (u32 EDT), d_map (f32 masked diameters) and d_sq (u32 propagated r^2).
+void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int mode, bool edt_only,
+               uint32_t* d_edt, float* d_map, uint32_t* d_sq, float scale, cudaStream_t s, PhaseResult& res) {
+  const size_t N = (size_t)dm.n();
+  const size_t bits_bytes = (size_t)dm.nw() * dm.h * dm.d * sizeof(uint32_t);
+  uint32_t* A = static_cast<uint32_t*>(ensure(ctx, ctx->dist, N * 4, "distance map"));
+  uint32_t* B = static_cast<uint32_t*>(ensure(ctx, ctx->dist2, N * 4, "distance map"));
+  void* scratch = ensure(ctx, ctx->stack, edt_scratch_bytes(dm), "envelope scratch");
+  uint32_t* selbits = static_cast<uint32_t*>(ensure(ctx, ctx->selbits, bits_bytes, "selection bits"));
+  Counters* ctr = static_cast<Counters*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
+  check(ctx, cudaMemsetAsync(ctr, 0, sizeof(Counters), s), "memset");
+
+  check(ctx, launch_edt_x(d_a, d_b, mode, dm, A, selbits, ctr, s, &ctx->launches), "edt x pass");
+  check(ctx, launch_edt_line(1, A, B, dm, scratch, ctr, s, &ctx->launches), "edt y pass");
+  uint32_t* E = d_edt ? d_edt : A;
+  check(ctx, launch_edt_line(2, B, E, dm, scratch, ctr, s, &ctx->launches), "edt z pass");
+
+  Counters hc;
+  check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
+  check(ctx, cudaStreamSynchronize(s), "edt");
+  res.sites = hc.sites;
+  res.selected = N - hc.sites;
+  res.rmax = hc.rmax;
+  if (hc.sites == 0) {
+    const int phase = (mode == SEL_BACKGROUND) ? BM_PHASE_BACKGROUND : BM_PHASE_FOREGROUND;
+    fail(ctx, BM_ERR_ALL_SELECTED,
+         "distance transform is undefined for an all-%s volume unless an exterior convention is specified",
+         phase_name(phase));
+  }
+  if (edt_only) return;
+
+  ensure_lut(ctx, hc.rmax);
+  const uint4* lut = static_cast<const uint4*>(ctx->lut.ptr);
+  uint2* ridges = static_cast<uint2*>(ensure(ctx, ctx->ridges, (res.selected + 1) * sizeof(uint2), "ridge list"));
+  check(ctx, launch_ridges(E, dm, lut, ridges, ctr, s, &ctx->launches), "ridge kernel");
+  uint32_t* F = d_sq ? d_sq : B;
+  check(ctx, cudaMemsetAsync(F, 0, N * 4, s), "memset");
+  check(ctx, launch_fill(ridges, ctr, res.selected, dm, F, s, &ctx->launches), "fill kernel");
+  uint32_t* posbits = static_cast<uint32_t*>(ensure(ctx, ctx->posbits, bits_bytes, "cleanup bits"));
+  check(ctx, launch_interior_bits(F, dm, posbits, s, &ctx->launches), "cleanup pass 1");
+  StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));
+  check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
+  check(ctx, launch_final(F, posbits, selbits, dm, lut, scale, d_map, acc, s, &ctx->launches), "cleanup pass 2");
+  check(ctx, cudaMemcpyAsync(&res.acc, acc, sizeof(StatsAccum), cudaMemcpyDeviceToHost, s), "stats readback");
+  check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
+  check(ctx, cudaStreamSynchronize(s), "local thickness");
+  res.ridges = hc.ridges;
+}
+
+// nonzero_stats from the exact sums (metrics.rs:228-241; quantile fields NaN).
+int finish_stats(bm_ctx* ctx, const StatsAccum& a, bm_stats* out) {
+  if (a.count == 0) {
+    set_err(ctx, "cannot compute statistics because the selected phase is empty");
+    return BM_ERR_EMPTY;
+  }
+  double sum, ss;
+  exact_sums_to_double(a, &sum, &ss);
+  const double c = (double)a.count;
+  const double mean = sum / c;
+  const double centered = (c * ss - sum * sum) / c;
+  const double sd = (a.count > 1 && centered > 0.0) ? std::sqrt(centered / (c - 1.0)) : 0.0;
+  float mxf;
+  std::memcpy(&mxf, &a.max_bits, 4);
+  if (out) {
+    out->count = a.count;
+    out->mean = mean;
+    out->standard_deviation = sd;
+    out->maximum = (double)mxf;
+    out->median = out->percentile_10 = out->percentile_25 = out->percentile_75 = out->percentile_90 = NAN;
+    out->interquartile_range = NAN;
+    out->coefficient_of_variation = sd / mean;
+    out->sum = sum;
+    out->sum_of_squares = ss;
+  }
+  return BM_OK;
+}
+
+template <class F>
+int guarded(bm_ctx* ctx, F&& f) {
+  if (!ctx) return BM_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->last_error.clear();
+  try {
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail(ctx, BM_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    }
+    return f();
+  } catch (const CallError& ce) {
+    return ce.status;
+  } catch (const std::bad_alloc&) {
+    ctx->last_error = "host allocation failed";
+    return BM_ERR_OOM;
+  }
+}
+
+cudaStream_t pick_stream(bm_ctx* ctx, void* stream) {
+  return stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+}
+
+int edt_device_impl(bm_ctx* ctx, const uint8_t* d_vol, Dims dm, int phase, uint32_t* d_out, cudaStream_t s) {
+  PhaseResult r;
+  run_phase(ctx, dm, d_vol, nullptr, phase == BM_PHASE_BACKGROUND ? SEL_BACKGROUND : SEL_FOREGROUND, true, d_out,
+            nullptr, nullptr, 1.0f, s, r);
+  return BM_OK;
+}
+
+int lt_device_impl(bm_ctx* ctx, const uint8_t* d_vol, Dims dm, int phase, float* d_out, uint32_t* d_sq,
+                   cudaStream_t s) {
+  PhaseResult r;
+  run_phase(ctx, dm, d_vol, nullptr, phase == BM_PHASE_BACKGROUND ? SEL_BACKGROUND : SEL_FOREGROUND, false,
+            nullptr, d_out, d_sq, 1.0f, s, r);
+  return BM_OK;
+}
+
+void check_phase(bm_ctx* ctx, int phase) {
+  if (phase != BM_PHASE_FOREGROUND && phase != BM_PHASE_BACKGROUND)
+    fail(ctx, BM_ERR_INVALID, "phase must be 0 (foreground) or 1 (background); got %d", phase);
+}
+
+__global__ void count_roi_kernel(const uint8_t* __restrict__ bone, const uint8_t* __restrict__ roi, long long n,
+                                 unsigned long long* __restrict__ out) {
+  unsigned long long in_roi = 0, bone_in = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const bool r = roi[i] != 0;
+    in_roi += r;
+    bone_in += (r && bone[i] != 0);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    in_roi += __shfl_xor_sync(0xffffffffu, in_roi, o);
+    bone_in += __shfl_xor_sync(0xffffffffu, bone_in, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (in_roi) atomicAdd(&out[0], in_roi);
+    if (bone_in) atomicAdd(&out[1], bone_in);
+  }
+}
+
+int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, Dims dm, double spacing,
+                     unsigned flags, bm_stats* th, bm_stats* sp, float* d_thmap, float* d_spmap, cudaStream_t s) {
+  // metrics.rs:70-78
+  if (!std::isfinite(spacing) || spacing <= 0.0)
+    fail(ctx, BM_ERR_SPACING, "voxel spacings must be finite and positive; got [%g, %g, %g]", spacing, spacing,
+         spacing);
+  if (flags & ~(unsigned)(BM_FLAG_QUANTILES | BM_FLAG_BONEJ_ROI))
+    fail(ctx, BM_ERR_INVALID, "unknown flags 0x%x", flags);
+  if (flags & BM_FLAG_QUANTILES) fail(ctx, BM_ERR_INVALID, "quantiles are not available in this build");
+  const long long N = dm.n();
+  unsigned long long* dcnt =
+      static_cast<unsigned long long*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
+  check(ctx, cudaMemsetAsync(dcnt, 0, 16, s), "memset");
+  count_roi_kernel<<<152 * 8, 256, 0, s>>>(d_bone, d_roi, N, dcnt);
+  ++ctx->launches;
+  check(ctx, cudaGetLastError(), "count kernel");
+  unsigned long long hc[2];
+  check(ctx, cudaMemcpyAsync(hc, dcnt, 16, cudaMemcpyDeviceToHost, s), "count readback");
+  check(ctx, cudaStreamSynchronize(s), "count kernel");
+  if (hc[0] == 0) fail(ctx, BM_ERR_ROI_EMPTY, "ROI mask contains no included voxels");
+  if ((flags & BM_FLAG_BONEJ_ROI) && hc[0] == (unsigned long long)N)
+    fail(ctx, BM_ERR_ROI_FULL, "BoneJ compatibility mode requires an ROI mask with both inside and outside voxels");
+  if (hc[1] == 0) fail(ctx, BM_ERR_NO_BONE, "ROI contains no bone voxels");
+  if (hc[1] == hc[0]) fail(ctx, BM_ERR_NO_MARROW, "ROI contains no marrow voxels");
+
+  const float scale = (float)spacing;  // metrics.rs:213
+  PhaseResult rb, rm;
+  run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, d_thmap, nullptr, scale, s, rb);
+  int st = finish_stats(ctx, rb.acc, th);
+  if (st) return st;
+  run_phase(ctx, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, d_spmap, nullptr, scale, s, rm);
+  return finish_stats(ctx, rm.acc, sp);
+}
+
+uint8_t* stage_input(bm_ctx* ctx, Buffer& b, const uint8_t* host, size_t n, cudaStream_t s) {
+  uint8_t* d = static_cast<uint8_t*>(ensure(ctx, b, n, "input volume"));
+  check(ctx, cudaMemcpyAsync(d, host, n, cudaMemcpyHostToDevice, s), "input upload");
+  return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bm_ctx_create(int device, bm_ctx** out) {
+  if (!out) return BM_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_err(nullptr, "no CUDA device available: %s", e == cudaSuccess ? "device count is 0" : cudaGetErrorString(e));
+    return BM_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev) {
+    set_err(nullptr, "device %d out of range (0..%d)", device, ndev - 1);
+    return BM_ERR_INVALID;
+  }
+  bm_ctx* ctx = new (std::nothrow) bm_ctx();
+  if (!ctx) return BM_ERR_OOM;
+  ctx->device = device;
+  e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_err(nullptr, "context creation failed: %s", cudaGetErrorString(e));
+    delete ctx;
+    return BM_ERR_CUDA;
+  }
+  *out = ctx;
+  return BM_OK;
+}
+
+int bm_ctx_trim(bm_ctx* ctx) {
+  return guarded(ctx, [&]() -> int {
+    cudaStreamSynchronize(ctx->stream);
+    Buffer* all[] = {&ctx->in_a, &ctx->in_b, &ctx->dist, &ctx->dist2, &ctx->stack, &ctx->fillmap, &ctx->selbits,
+                     &ctx->posbits, &ctx->ridges, &ctx->accum, &ctx->outmap, &ctx->outmap2};
+    for (Buffer* b : all) release(*b);
+    return BM_OK;
+  });
+}
+
+void bm_ctx_destroy(bm_ctx* ctx) {
+  if (!ctx) return;
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    Buffer* all[] = {&ctx->lut,     &ctx->in_a,   &ctx->in_b,     &ctx->dist,    &ctx->dist2,
+                     &ctx->stack,   &ctx->fillmap, &ctx->selbits, &ctx->posbits, &ctx->ridges,
+                     &ctx->counters, &ctx->accum,  &ctx->outmap,  &ctx->outmap2, &ctx->host_pinned};
+    for (Buffer* b : all) release(*b);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+}
+
+const char* bm_status_string(int status) {
+  switch (status) {
+    case BM_OK: return "ok";
+    case BM_ERR_ALL_SELECTED: return "all voxels selected";
+    case BM_ERR_DIMS: return "invalid dimensions";
+    case BM_ERR_OOM: return "out of device memory";
+    case BM_ERR_CUDA: return "CUDA error";
+    case BM_ERR_TIMEOUT: return "device wait timed out";
+    case BM_ERR_INVALID: return "invalid argument";
+    case BM_ERR_EMPTY: return "empty phase";
+    case BM_ERR_ROI_EMPTY: return "empty ROI";
+    case BM_ERR_NO_BONE: return "no bone in ROI";
+    case BM_ERR_NO_MARROW: return "no marrow in ROI";
+    case BM_ERR_NO_DEVICE: return "no CUDA device";
+    case BM_ERR_SPACING: return "invalid spacing";
+    case BM_ERR_ROI_FULL: return "ROI has no outside voxels";
+    case BM_ERR_BUSY: return "busy";
+    default: return "unknown status";
+  }
+}
+
+size_t bm_last_error(const bm_ctx* ctx, char* buf, size_t len) {
+  const std::string& s = ctx ? ctx->last_error : g_create_error;
+  if (buf && len) {
+    const size_t n = s.size() < len - 1 ? s.size() : len - 1;
+    std::memcpy(buf, s.data(), n);
+    buf[n] = 0;
+  }
+  return s.size();
+}
+
+uint64_t bm_ctx_launch_count(const bm_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int bm_edt_sq_device(bm_ctx* ctx, const uint8_t* d_volume, size_t width, size_t height, size_t depth, int phase,
+                     uint32_t* d_out, void* stream) {
+  return guarded(ctx, [&]() -> int {
+    if (!d_volume || !d_out) fail(ctx, BM_ERR_INVALID, "null pointer");
+    check_phase(ctx, phase);
+    const Dims dm = check_dims(ctx, width, height, depth);
+    return edt_device_impl(ctx, d_volume, dm, phase, d_out, pick_stream(ctx, stream));
+  });
+}
+
+int bm_edt_sq(bm_ctx* ctx, const uint8_t* volume, size_t width, size_t height, size_t depth, int phase,
+              uint32_t* out) {
+  return guarded(ctx, [&]() -> int {
+    if (!volume || !out) fail(ctx, BM_ERR_INVALID, "null pointer");
+    check_phase(ctx, phase);
+    const Dims dm = check_dims(ctx, width, height, depth);
+    const size_t N = (size_t)dm.n();
+    cudaStream_t s = ctx->stream;
+    uint8_t* d_in = stage_input(ctx, ctx->in_a, volume, N, s);
+    uint32_t* d_out = static_cast<uint32_t*>(ensure(ctx, ctx->fillmap, N * 4, "output"));
+    edt_device_impl(ctx, d_in, dm, phase, d_out, s);
+    check(ctx, cudaMemcpyAsync(out, d_out, N * 4, cudaMemcpyDeviceToHost, s), "result download");
+    check(ctx, cudaStreamSynchronize(s), "result download");
+    return BM_OK;
+  });
+}
+
+int bm_local_thickness_device(bm_ctx* ctx, const uint8_t* d_volume, size_t width, size_t height, size_t depth,
+                              int phase, float* d_out, uint32_t* d_squared_thickness, void* stream) {
+  return guarded(ctx, [&]() -> int {
+    if (!d_volume || !d_out) fail(ctx, BM_ERR_INVALID, "null pointer");
+    check_phase(ctx, phase);
+    const Dims dm = check_dims(ctx, width, height, depth);
+    return lt_device_impl(ctx, d_volume, dm, phase, d_out, d_squared_thickness, pick_stream(ctx, stream));
+  });
+}
+
+int bm_local_thickness(bm_ctx* ctx, const uint8_t* volume, size_t width, size_t height, size_t depth, int phase,
+                       float* out, uint32_t* squared_thickness) {
+  return guarded(ctx, [&]() -> int {
+    if (!volume || !out) fail(ctx, BM_ERR_INVALID, "null pointer");
+    check_phase(ctx, phase);
+    const Dims dm = check_dims(ctx, width, height, depth);
+    const size_t N = (size_t)dm.n();
+    cudaStream_t s = ctx->stream;
+    uint8_t* d_in = stage_input(ctx, ctx->in_a, volume, N, s);
+    float* d_out = static_cast<float*>(ensure(ctx, ctx->outmap, N * 4, "output"));
+    uint32_t* d_sq = squared_thickness ? static_cast<uint32_t*>(ensure(ctx, ctx->fillmap, N * 4, "output")) : nullptr;
+    lt_device_impl(ctx, d_in, dm, phase, d_out, d_sq, s);
+    check(ctx, cudaMemcpyAsync(out, d_out, N * 4, cudaMemcpyDeviceToHost, s), "result download");
+    if (squared_thickness)
+      check(ctx, cudaMemcpyAsync(squared_thickness, d_sq, N * 4, cudaMemcpyDeviceToHost, s), "result download");
+    check(ctx, cudaStreamSynchronize(s), "result download");
+    return BM_OK;
+  });
+}
+
+int bm_tbth_tbsp_device(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, size_t width, size_t height,
+                        size_t depth, double spacing_um, unsigned flags, bm_stats* thickness, bm_stats* spacing,
+                        float* d_thickness_map, float* d_spacing_map, void* stream) {
+  return guarded(ctx, [&]() -> int {
+    if (!d_bone || !d_roi) fail(ctx, BM_ERR_INVALID, "null pointer");
+    const Dims dm = check_dims(ctx, width, height, depth);
+    return tbth_device_impl(ctx, d_bone, d_roi, dm, spacing_um, flags, thickness, spacing, d_thickness_map,
+                            d_spacing_map, pick_stream(ctx, stream));
+  });
+}
+
+int bm_tbth_tbsp(bm_ctx* ctx, const uint8_t* bone, const uint8_t* roi, size_t width, size_t height, size_t depth,
+                 double spacing_um, unsigned flags, bm_stats* thickness, bm_stats* spacing, float* thickness_map,
+                 float* spacing_map) {
+  return guarded(ctx, [&]() -> int {
+    if (!bone || !roi) fail(ctx, BM_ERR_INVALID, "null pointer");
+    const Dims dm = check_dims(ctx, width, height, depth);
+    const size_t N = (size_t)dm.n();
+    cudaStream_t s = ctx->stream;
+    const uint8_t* d_bone = stage_input(ctx, ctx->in_a, bone, N, s);
+    const uint8_t* d_roi = stage_input(ctx, ctx->in_b, roi, N, s);
+    float* d_th = thickness_map ? static_cast<float*>(ensure(ctx, ctx->outmap, N * 4, "output")) : nullptr;
+    float* d_sp = spacing_map ? static_cast<float*>(ensure(ctx, ctx->outmap2, N * 4, "output")) : nullptr;
+    int st = tbth_device_impl(ctx, d_bone, d_roi, dm, spacing_um, flags, thickness, spacing, d_th, d_sp, s);
+    if (st) return st;
+    if (thickness_map)
+      check(ctx, cudaMemcpyAsync(thickness_map, d_th, N * 4, cudaMemcpyDeviceToHost, s), "result download");
+    if (spacing_map)
+      check(ctx, cudaMemcpyAsync(spacing_map, d_sp, N * 4, cudaMemcpyDeviceToHost, s), "result download");
+    check(ctx, cudaStreamSynchronize(s), "result download");
+    return BM_OK;
+  });
+}
+
+}  // extern "C"

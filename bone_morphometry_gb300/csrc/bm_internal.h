@@ -1,0 +1,82 @@
+// Internal definitions shared by the CUDA translation units of libbm_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+
+#include "bm.h"
+
+namespace bm {
+
+constexpr uint32_t kInfSq = 0xFFFFFFFFu;  // "no site on this line" in the EDT passes
+
+// Selection of the phase from the inputs, evaluated inside the first EDT pass
+// (edt.rs:19-24 and volume.rs:84-105).
+enum SelMode : int {
+  SEL_FOREGROUND = 0,  // a != 0
+  SEL_BACKGROUND = 1,  // a == 0
+  SEL_BONE_IN_ROI = 2,    // roi != 0 && bone != 0       (Tb.Th phase)
+  SEL_MARROW_IN_ROI = 3,  // roi != 0 && bone == 0       (Tb.Sp phase)
+};
+
+struct Dims {
+  int w, h, d;
+  __host__ __device__ long long n() const { return (long long)w * h * d; }
+  __host__ __device__ int nw() const { return (w + 31) >> 5; }  // 32-bit words per x row of a bitmask
+};
+
+// Exact-sum accumulator for the statistics: per f32 exponent the sum of the
+// 24-bit mantissas and of the 48-bit squared mantissas (split into two 24-bit
+// halves), plus count and maximum.  Exact for < 2^34 values.
+struct StatsAccum {
+  unsigned long long sum_m[256];
+  unsigned long long sq_hi[256];
+  unsigned long long sq_lo[256];
+  unsigned long long count;
+  unsigned int max_bits;
+  unsigned int pad;
+};
+
+// Device scratch owned by a context, grown on demand and reused across calls.
+struct Buffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct Counters {  // device-side counters of one phase
+  unsigned long long sites;     // non-selected voxels
+  unsigned long long selected;  // selected voxels
+  unsigned long long ridges;
+  unsigned int rmax;
+  unsigned int status;  // nonzero: a bounded wait gave up / capacity exceeded
+};
+
+}  // namespace bm
+
+struct bm_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string last_error;
+  unsigned long long launches = 0;
+  int num_sms = 0;
+
+  // cached search-template table: lut[r2] = {t100, t110, t111, 0}
+  bm::Buffer lut;
+  uint32_t lut_max = 0;  // entries 0..lut_max are valid
+
+  bm::Buffer in_a, in_b;       // staged host inputs
+  bm::Buffer dist, dist2;      // u32 EDT ping/pong
+  bm::Buffer stack;            // EDT line scratch
+  bm::Buffer fillmap;          // u32 propagated r^2
+  bm::Buffer selbits, posbits; // row-padded bitmasks
+  bm::Buffer ridges;           // ridge records
+  bm::Buffer counters;         // bm::Counters
+  bm::Buffer accum;            // bm::StatsAccum
+  bm::Buffer outmap;           // f32 output staging
+  bm::Buffer outmap2;
+  bm::Buffer host_pinned;      // pinned staging for small readbacks
+};

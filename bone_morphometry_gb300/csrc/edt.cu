@@ -1,0 +1,275 @@
+// Exact squared Euclidean distance transform on sm_103a (edt.rs:57-156).
+//
+// The reference computes the Felzenszwalb-Huttenlocher lower envelope in f64
+// with INF = 1e30 and rounds; on integer inputs every comparison it makes is
+// exact and INF parabolas never reach the envelope inside a line that has a
+// finite one, so its output is the mathematically exact squared EDT.  The GPU
+// computes the same values with integers only:
+//   pass x : distance to the nearest non-selected voxel of the row, from a
+//            bitmask of the row (ballot + clz/ffs), squared;
+//   pass y, z : lower envelope of the parabolas (q - p)^2 + f(p) with the
+//            intersection test done by int64 cross-multiplication; lines
+//            whose every entry is "no site" (kInfSq) stay kInfSq.
+#include <climits>
+
+#include "kernels.h"
+
+namespace bm {
+
+namespace {
+
+template <int MODE>
+__device__ __forceinline__ bool selected_at(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b,
+                                            long long i) {
+  if (MODE == SEL_FOREGROUND) return a[i] != 0;
+  if (MODE == SEL_BACKGROUND) return a[i] == 0;
+  if (MODE == SEL_BONE_IN_ROI) return b[i] != 0 && a[i] != 0;
+  return b[i] != 0 && a[i] == 0;
+}
+
+constexpr int kXWarps = 8;
+
+// One warp per x row.  Shared memory per warp: site bitmask of the row and, per
+// word, the nearest non-empty word at-or-before / at-or-after it.
+template <int MODE>
+__global__ void __launch_bounds__(kXWarps * 32)
+edt_x_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, Dims dm, uint32_t* __restrict__ out,
+             uint32_t* __restrict__ selbits, Counters* __restrict__ ctr) {
+  extern __shared__ uint32_t smem[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nw = dm.nw();
+  uint32_t* mask = smem + (size_t)warp * 3 * nw;
+  int* prevnz = reinterpret_cast<int*>(mask + nw);
+  int* nextnz = prevnz + nw;
+  const long long rows = (long long)dm.h * dm.d;
+  unsigned long long sites = 0;
+
+  for (long long row = (long long)blockIdx.x * kXWarps + warp; row < rows;
+       row += (long long)gridDim.x * kXWarps) {
+    const long long base = row * dm.w;
+    for (int c = 0; c < nw; ++c) {
+      const int x = c * 32 + lane;
+      const bool in = x < dm.w;
+      const bool s = in && selected_at<MODE>(a, b, base + x);
+      const unsigned site = __ballot_sync(0xffffffffu, in && !s);
+      const unsigned selw = __ballot_sync(0xffffffffu, s);
+      if (lane == 0) {
+        mask[c] = site;
+        selbits[row * nw + c] = selw;
+        sites += __popc(site);
+      }
+    }
+    __syncwarp();
+    int carry = -1;
+    for (int c0 = 0; c0 < nw; c0 += 32) {
+      const int c = c0 + lane;
+      int v = (c < nw && mask[c] != 0u) ? c : -1;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v = max(v, t);
+      }
+      v = max(v, carry);
+      if (c < nw) prevnz[c] = v;
+      carry = __shfl_sync(0xffffffffu, v, 31);
+    }
+    carry = INT_MAX;
+    for (int c0 = ((nw - 1) >> 5) << 5; c0 >= 0; c0 -= 32) {
+      const int c = c0 + lane;
+      int v = (c < nw && mask[c] != 0u) ? c : INT_MAX;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_down_sync(0xffffffffu, v, o);
+        if (lane + o < 32) v = min(v, t);
+      }
+      v = min(v, carry);
+      if (c < nw) nextnz[c] = v;
+      carry = __shfl_sync(0xffffffffu, v, 0);
+    }
+    __syncwarp();
+    for (int c = 0; c < nw; ++c) {
+      const int x = c * 32 + lane;
+      if (x < dm.w) {
+        const uint32_t m = mask[c];
+        uint32_t val = 0;
+        if (!((m >> lane) & 1u)) {
+          int left = -1, right = -1;
+          const uint32_t lo = m & ((1u << lane) - 1u);
+          if (lo) {
+            left = c * 32 + 31 - __clz(lo);
+          } else if (c > 0) {
+            const int p = prevnz[c - 1];
+            if (p >= 0) left = p * 32 + 31 - __clz(mask[p]);
+          }
+          const uint32_t hi = (lane == 31) ? 0u : (m & ~((2u << lane) - 1u));
+          if (hi) {
+            right = c * 32 + __ffs(hi) - 1;
+          } else if (c + 1 < nw) {
+            const int p = nextnz[c + 1];
+            if (p != INT_MAX) right = p * 32 + __ffs(mask[p]) - 1;
+          }
+          int g = INT_MAX;
+          if (left >= 0) g = x - left;
+          if (right >= 0) g = min(g, right - x);
+          val = (g == INT_MAX) ? kInfSq : (uint32_t)g * (uint32_t)g;
+        }
+        out[base + x] = val;
+      }
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && sites) atomicAdd(&ctr->sites, sites);
+}
+
+// One thread per line; consecutive threads take consecutive x so that every
+// load and store of the line data is a coalesced row.  The envelope stack
+// (position, f) lives in global scratch, k-major, and is cached by L1/L2.
+__global__ void __launch_bounds__(256)
+edt_line_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int n, long long stride, int w,
+                long long outer, long long nlines, uint32_t* __restrict__ spos, uint32_t* __restrict__ sf,
+                Counters* __restrict__ ctr, int track_max) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t localmax = 0;
+  if (t < nlines) {
+    const long long base = (t / w) * outer + (t % w);
+    int k = -1;
+    long long p1 = 0, F1 = 0;  // stack top
+    long long p0 = 0, F0 = 0;  // entry below the top (valid when k >= 1)
+    for (int q = 0; q < n; ++q) {
+      const uint32_t fq = in[base + (long long)q * stride];
+      if (fq == kInfSq) continue;
+      const long long Fq = (long long)fq + (long long)q * q;
+      while (k >= 1 && (Fq - F1) * (p1 - p0) <= (F1 - F0) * ((long long)q - p1)) {
+        --k;
+        p1 = p0;
+        F1 = F0;
+        if (k >= 1) {
+          p0 = spos[(long long)(k - 1) * nlines + t];
+          F0 = (long long)sf[(long long)(k - 1) * nlines + t] + p0 * p0;
+        }
+      }
+      ++k;
+      spos[(long long)k * nlines + t] = (uint32_t)q;
+      sf[(long long)k * nlines + t] = fq;
+      p0 = p1;
+      F0 = F1;
+      p1 = q;
+      F1 = Fq;
+    }
+    if (k < 0) {
+      for (int q = 0; q < n; ++q) out[base + (long long)q * stride] = kInfSq;
+    } else {
+      int j = 0;
+      long long pj = spos[t];
+      uint32_t fj = sf[t];
+      long long Fj = (long long)fj + pj * pj;
+      long long pn = 0, Fn = 0;
+      uint32_t fn = 0;
+      if (k >= 1) {
+        pn = spos[nlines + t];
+        fn = sf[nlines + t];
+        Fn = (long long)fn + pn * pn;
+      }
+      for (int q = 0; q < n; ++q) {
+        while (j < k && (Fn - Fj) < 2LL * q * (pn - pj)) {
+          ++j;
+          pj = pn;
+          fj = fn;
+          Fj = Fn;
+          if (j < k) {
+            pn = spos[(long long)(j + 1) * nlines + t];
+            fn = sf[(long long)(j + 1) * nlines + t];
+            Fn = (long long)fn + pn * pn;
+          }
+        }
+        const long long dq = q - pj;
+        const uint32_t v = (uint32_t)(dq * dq) + fj;
+        out[base + (long long)q * stride] = v;
+        localmax = max(localmax, v);
+      }
+    }
+  }
+  if (track_max) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) localmax = max(localmax, __shfl_xor_sync(0xffffffffu, localmax, o));
+    if ((threadIdx.x & 31) == 0 && localmax) atomicMax(&ctr->rmax, localmax);
+  }
+}
+
+}  // namespace
+
+size_t edt_scratch_bytes(Dims dm) {
+  // two u32 arrays (position, f) of line-length x line-count for the larger pass
+  const long long y_pass = (long long)dm.h * dm.w * dm.d;
+  return (size_t)y_pass * 2 * sizeof(uint32_t);
+}
+
+cudaError_t launch_edt_x(const uint8_t* a, const uint8_t* b, int mode, Dims dm, uint32_t* out,
+                         uint32_t* selbits, Counters* ctr, cudaStream_t s, unsigned long long* launches) {
+  const long long rows = (long long)dm.h * dm.d;
+  long long blocks = (rows + kXWarps - 1) / kXWarps;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  const size_t smem = (size_t)kXWarps * 3 * dm.nw() * sizeof(uint32_t);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaSuccess;
+    switch (mode) {
+      case SEL_FOREGROUND:
+        e = cudaFuncSetAttribute(edt_x_kernel<SEL_FOREGROUND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        break;
+      case SEL_BACKGROUND:
+        e = cudaFuncSetAttribute(edt_x_kernel<SEL_BACKGROUND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        break;
+      case SEL_BONE_IN_ROI:
+        e = cudaFuncSetAttribute(edt_x_kernel<SEL_BONE_IN_ROI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        break;
+      default:
+        e = cudaFuncSetAttribute(edt_x_kernel<SEL_MARROW_IN_ROI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        break;
+    }
+    if (e != cudaSuccess) return e;
+  }
+  switch (mode) {
+    case SEL_FOREGROUND:
+      edt_x_kernel<SEL_FOREGROUND><<<(unsigned)blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+      break;
+    case SEL_BACKGROUND:
+      edt_x_kernel<SEL_BACKGROUND><<<(unsigned)blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+      break;
+    case SEL_BONE_IN_ROI:
+      edt_x_kernel<SEL_BONE_IN_ROI><<<(unsigned)blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+      break;
+    default:
+      edt_x_kernel<SEL_MARROW_IN_ROI><<<(unsigned)blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+      break;
+  }
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_edt_line(int axis, const uint32_t* in, uint32_t* out, Dims dm, void* scratch, Counters* ctr,
+                            cudaStream_t s, unsigned long long* launches) {
+  int n;
+  long long stride, outer, nlines;
+  if (axis == 1) {
+    n = dm.h;
+    stride = dm.w;
+    outer = (long long)dm.w * dm.h;
+    nlines = (long long)dm.w * dm.d;
+  } else {
+    n = dm.d;
+    stride = (long long)dm.w * dm.h;
+    outer = dm.w;
+    nlines = (long long)dm.w * dm.h;
+  }
+  uint32_t* spos = static_cast<uint32_t*>(scratch);
+  uint32_t* sf = spos + (size_t)nlines * n;
+  const long long blocks = (nlines + 255) / 256;
+  edt_line_kernel<<<(unsigned)blocks, 256, 0, s>>>(in, out, n, stride, dm.w, outer, nlines, spos, sf, ctr,
+                                                   axis == 2 ? 1 : 0);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+}  // namespace bm

@@ -1,0 +1,145 @@
+/*
+ * bm.h -- C ABI of the GB300 (sm_103a) Tb.Th / Tb.Sp library.
+ *
+ * This is the drop-in boundary for the trabecular thickness / separation
+ * path of bone-morphometry v0.7.0-rc.3 (Rust).  Every entry point is plain C:
+ * pointers, sizes and status codes, no CUDA or C++ types.  A Rust binding
+ * (extern "C" block + the two module functions re-implemented on top of it)
+ * is shown in INTEGRATION.md.
+ *
+ * Volumes use the reference layout (volume.rs:44-46): index = (z*height + y)*width + x,
+ * x fastest, one byte per voxel.  Host-pointer entry points copy inputs to the
+ * device and results back; *_device entry points take device pointers and a
+ * cudaStream_t passed as void* (NULL = the context's own stream) and return
+ * once the results are complete (stream synchronised).
+ *
+ * Errors follow the reference's bails (anyhow::bail!); bm_last_error() returns
+ * the reference's message text for the last failing call on the context.
+ *
+ * Thread safety: a context serialises its calls with an internal mutex; use
+ * one context per host thread for concurrency.  There is no CPU fallback: with
+ * no usable GPU, bm_ctx_create fails with BM_ERR_NO_DEVICE.
+ */
+#ifndef BM_H
+#define BM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BM_ABI_VERSION 1
+
+typedef enum bm_status {
+  BM_OK = 0,
+  BM_ERR_ALL_SELECTED = 1, /* edt.rs:61-66: EDT of an all-selected volume              */
+  BM_ERR_DIMS = 2,         /* volume.rs:12-34: a dimension < 2, or size overflow        */
+  BM_ERR_OOM = 3,          /* device allocation failed                                   */
+  BM_ERR_CUDA = 4,         /* any other CUDA runtime error                                */
+  BM_ERR_TIMEOUT = 5,      /* a bounded device-side wait ran out                         */
+  BM_ERR_INVALID = 6,      /* null pointer, bad phase / flag, shape mismatch (metrics.rs:79-89) */
+  BM_ERR_EMPTY = 7,        /* metrics.rs:228-230: no finite positive map value           */
+  BM_ERR_ROI_EMPTY = 8,    /* metrics.rs:90-92: ROI has no included voxel                */
+  BM_ERR_NO_BONE = 9,      /* metrics.rs:99-101                                           */
+  BM_ERR_NO_MARROW = 10,   /* metrics.rs:102-104                                          */
+  BM_ERR_NO_DEVICE = 11,   /* no CUDA device / driver                                    */
+  BM_ERR_SPACING = 12,     /* metrics.rs:70-78: spacing not finite and positive          */
+  BM_ERR_ROI_FULL = 13,    /* metrics.rs:93-95: BoneJ mode needs inside and outside voxels */
+  BM_ERR_BUSY = 14         /* server queue full / over budget (serving only)             */
+} bm_status;
+
+/* edt.rs:8-24 -- Foreground selects value != 0, Background selects value == 0. */
+typedef enum bm_phase { BM_PHASE_FOREGROUND = 0, BM_PHASE_BACKGROUND = 1 } bm_phase;
+
+/* metrics.rs:27-38 (DistributionStats), in micrometres.  Quantile fields are
+ * NaN unless BM_FLAG_QUANTILES was given (metrics.rs:242-255); then
+ * interquartile_range = p75 - p25 and coefficient_of_variation = sd / mean.
+ * sum and sum_of_squares are the exact sums of the scaled f32 values rounded
+ * once to f64 (the reference accumulates them sequentially). */
+typedef struct bm_stats {
+  uint64_t count;
+  double mean;
+  double standard_deviation;
+  double maximum;
+  double median;
+  double percentile_10;
+  double percentile_25;
+  double percentile_75;
+  double percentile_90;
+  double interquartile_range;
+  double coefficient_of_variation;
+  double sum;
+  double sum_of_squares;
+} bm_stats;
+
+/* Flags for bm_tbth_tbsp*. */
+#define BM_FLAG_QUANTILES 1u  /* also compute median / P10 / P25 / P75 / P90 (Standard, Experimental modes) */
+#define BM_FLAG_BONEJ_ROI 2u  /* metrics.rs:93-95: reject an ROI without outside voxels      */
+
+typedef struct bm_ctx bm_ctx;
+
+/* Create a context on CUDA device `device` (its own stream, cached device
+ * buffers, the cached search-template table). */
+int bm_ctx_create(int device, bm_ctx** out);
+void bm_ctx_destroy(bm_ctx* ctx);
+
+/* Human-readable name of a status code (static string). */
+const char* bm_status_string(int status);
+
+/* Copy the last error message of `ctx` into buf (NUL-terminated, truncated to
+ * len); returns the full message length.  ctx may be NULL for errors raised
+ * by bm_ctx_create. */
+size_t bm_last_error(const bm_ctx* ctx, char* buf, size_t len);
+
+/* Release every cached device buffer of the context (kept otherwise, grown on
+ * demand, so repeated calls of one shape allocate nothing). */
+int bm_ctx_trim(bm_ctx* ctx);
+
+/* Exact squared Euclidean distance transform of the selected phase.
+ * Replaces edt.rs:57-60 `euclidean_distance_transform_squared(&BinaryVolume,
+ * Phase) -> Result<Vec<u32>>`: out[i] = squared distance (voxel units) from a
+ * selected voxel's centre to the nearest non-selected voxel centre, 0 for
+ * non-selected voxels; no exterior halo.  BM_ERR_ALL_SELECTED when every voxel
+ * is selected; BM_ERR_DIMS when a dimension is < 2 (volume.rs:27-34). */
+int bm_edt_sq(bm_ctx* ctx, const uint8_t* volume, size_t width, size_t height, size_t depth,
+              int phase, uint32_t* out);
+
+/* Local thickness map in voxel units (diameters).
+ * Replaces local_thickness.rs:16 `local_thickness(&BinaryVolume, Phase) ->
+ * Result<Vec<f32>>`.  out[i] is 0 for non-selected voxels.  When
+ * squared_thickness is not NULL it receives the propagated squared-thickness
+ * map (u32 r^2 before the square root, unmasked; local_thickness.rs:169-202). */
+int bm_local_thickness(bm_ctx* ctx, const uint8_t* volume, size_t width, size_t height,
+                       size_t depth, int phase, float* out, uint32_t* squared_thickness);
+
+/* Tb.Th and Tb.Sp of one specimen.  Replaces the hot block of
+ * metrics.rs:64-121 (`analyze`): validity bails, phase_inside for bone and
+ * marrow (volume.rs:84-105), local_thickness of each (metrics.rs:111,119) and
+ * nonzero_stats scaled by spacing (metrics.rs:112-116,120).  bone and roi are
+ * binary (any non-zero value counts).  thickness_map / spacing_map may be NULL;
+ * otherwise they receive the masked f32 diameter maps in voxel units. */
+int bm_tbth_tbsp(bm_ctx* ctx, const uint8_t* bone, const uint8_t* roi, size_t width, size_t height,
+                 size_t depth, double spacing_um, unsigned flags, bm_stats* thickness,
+                 bm_stats* spacing, float* thickness_map, float* spacing_map);
+
+/* Device-pointer variants (inputs and outputs in device memory). */
+int bm_edt_sq_device(bm_ctx* ctx, const uint8_t* d_volume, size_t width, size_t height,
+                     size_t depth, int phase, uint32_t* d_out, void* stream);
+int bm_local_thickness_device(bm_ctx* ctx, const uint8_t* d_volume, size_t width, size_t height,
+                              size_t depth, int phase, float* d_out, uint32_t* d_squared_thickness,
+                              void* stream);
+int bm_tbth_tbsp_device(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, size_t width,
+                        size_t height, size_t depth, double spacing_um, unsigned flags,
+                        bm_stats* thickness, bm_stats* spacing, float* d_thickness_map,
+                        float* d_spacing_map, void* stream);
+
+/* Kernel launches issued by this context since creation (library kernels only). */
+uint64_t bm_ctx_launch_count(const bm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BM_H */

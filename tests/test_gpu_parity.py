@@ -1,0 +1,189 @@
+"""GPU parity through the C ABI against the CPU oracle (bit-exact maps, stats
+within the stated tolerance).  Marked gpu."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from bone_morphometry_gb300 import (BinaryVolume, BoneMorphometryError, Phase, analyze_thickness,
+                                    euclidean_distance_transform_squared, local_thickness)
+from bone_morphometry_gb300 import _lib
+from bone_morphometry_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+# Relative tolerance of the Tb.Th / Tb.Sp mean, SD and max against the
+# reference's own sequential f64 accumulation.  The GPU sums exactly (bitwise
+# equal to oracle.exact_moment_sums + the reference formulas); the sequential
+# sum of n positive terms differs from the exact one by at most ~n*eps, and the
+# SD formula amplifies that by ~ mean^2 / var.
+def seq_tol(n, amplification=1.0):
+    return max(1e-12, 4.0 * n * 2.0 ** -53 * amplification)
+
+
+def rand_volume(shape, p, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.random(shape) < p).astype(np.uint8) * np.uint8(255)
+
+
+def blob_volume(shape, sigma, frac, seed):
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    f = gaussian_filter(rng.standard_normal(shape).astype(np.float32), sigma)
+    thr = np.quantile(f, 1 - frac)
+    return (f > thr).astype(np.uint8)
+
+
+EDT_CASES = [
+    ((3, 3, 3), 0.5, 1), ((2, 2, 2), 0.5, 2), ((5, 7, 11), 0.3, 3), ((33, 31, 65), 0.9, 4),
+    ((17, 129, 40), 0.97, 5), ((64, 64, 64), 0.5, 6), ((2, 300, 3), 0.99, 7), ((41, 2, 257), 0.8, 8),
+    ((16, 16, 1100), 0.995, 9),
+]
+
+
+@pytest.mark.parametrize("shape,p,seed", EDT_CASES)
+@pytest.mark.parametrize("phase", [Phase.FOREGROUND, Phase.BACKGROUND])
+def test_edt_bitwise(gpu_ctx, shape, p, seed, phase):
+    vol = rand_volume(shape, p, seed)
+    sel = vol != 0 if phase == Phase.FOREGROUND else vol == 0
+    if sel.all():
+        vol.flat[0] = 0 if phase == Phase.FOREGROUND else 255
+    got = euclidean_distance_transform_squared(vol, phase, ctx=gpu_ctx)
+    ref = O.edt_sq(vol, int(phase))
+    assert np.array_equal(got, ref)
+
+
+def test_edt_kat_center(gpu_ctx):
+    # edt.rs:240-274
+    data = np.ones((3, 3, 3), np.uint8)
+    data[1, 1, 1] = 0
+    e = euclidean_distance_transform_squared(data, Phase.FOREGROUND, ctx=gpu_ctx).ravel()
+    assert e[13] == 0 and e[12] == 1 and e[0] == 3
+    e = euclidean_distance_transform_squared(1 - data, Phase.BACKGROUND, ctx=gpu_ctx).ravel()
+    assert e[13] == 0 and e[12] == 1 and e[0] == 3
+
+
+def test_edt_single_site_far(gpu_ctx):
+    vol = np.ones((40, 70, 90), np.uint8)
+    vol[0, 0, 0] = 0
+    assert np.array_equal(euclidean_distance_transform_squared(vol, ctx=gpu_ctx), O.edt_sq(vol))
+
+
+def test_errors(gpu_ctx):
+    with pytest.raises(BoneMorphometryError, match="all-foreground volume") as ei:
+        euclidean_distance_transform_squared(np.ones((4, 4, 4), np.uint8), ctx=gpu_ctx)
+    assert ei.value.status == _lib.BM_ERR_ALL_SELECTED
+    with pytest.raises(BoneMorphometryError, match="all-background volume"):
+        local_thickness(np.zeros((4, 4, 4), np.uint8), Phase.BACKGROUND, ctx=gpu_ctx)
+    with pytest.raises(BoneMorphometryError, match="at least 2"):
+        euclidean_distance_transform_squared(np.ones((1, 4, 4), np.uint8), ctx=gpu_ctx)
+    bone = np.zeros((6, 6, 6), np.uint8)
+    roi = np.zeros((6, 6, 6), np.uint8)
+    with pytest.raises(BoneMorphometryError, match="ROI mask contains no included voxels"):
+        analyze_thickness(bone, roi, 1.0, ctx=gpu_ctx)
+    roi[1:5, 1:5, 1:5] = 1
+    with pytest.raises(BoneMorphometryError, match="ROI contains no bone voxels"):
+        analyze_thickness(bone, roi, 1.0, ctx=gpu_ctx)
+    bone[:] = 255
+    with pytest.raises(BoneMorphometryError, match="ROI contains no marrow voxels"):
+        analyze_thickness(bone, roi, 1.0, ctx=gpu_ctx)
+    with pytest.raises(BoneMorphometryError, match="finite and positive"):
+        analyze_thickness(bone, roi, float("nan"), ctx=gpu_ctx)
+    # the context stays usable after errors
+    vol = rand_volume((9, 9, 9), 0.5, 0)
+    assert np.array_equal(euclidean_distance_transform_squared(vol, ctx=gpu_ctx), O.edt_sq(vol))
+
+
+LT_CASES = [
+    ("kat", None), ("rand", ((20, 21, 22), 0.6, 11)), ("rand", ((7, 40, 33), 0.3, 12)),
+    ("blob", ((48, 40, 56), 2.0, 0.3, 13)), ("blob", ((64, 64, 64), 3.0, 0.7, 14)),
+    ("blob", ((30, 90, 17), 1.5, 0.5, 15)),
+]
+
+
+@pytest.mark.parametrize("kind,args", LT_CASES)
+@pytest.mark.parametrize("phase", [Phase.FOREGROUND, Phase.BACKGROUND])
+def test_local_thickness_bitwise(gpu_ctx, kind, args, phase):
+    if kind == "kat":
+        vol = np.zeros((3, 3, 3), np.uint8)
+        vol[1, 1, 1] = 1
+        if phase == Phase.BACKGROUND:
+            vol = 1 - vol
+    elif kind == "rand":
+        vol = rand_volume(*args)
+    else:
+        vol = blob_volume(*args)
+    ref = O.local_thickness(vol, int(phase))
+    got, sq = local_thickness(vol, phase, ctx=gpu_ctx, return_squared=True)
+    assert np.array_equal(sq, ref.propagated)
+    assert np.array_equal(got.view(np.uint32), ref.thickness.view(np.uint32))
+
+
+def test_isolated_voxel_has_diameter_two(gpu_ctx):
+    # local_thickness.rs:364-374
+    vol = np.zeros((3, 3, 3), np.uint8)
+    vol[1, 1, 1] = 1
+    t = local_thickness(vol, ctx=gpu_ctx).ravel()
+    assert t[13] == 2.0 and (t > 0).sum() == 1
+
+
+def test_background_matches_complement(gpu_ctx):
+    # local_thickness.rs:376-393
+    data = np.zeros((5, 5, 5), np.uint8)
+    data[1:4, 1:4, 1:4] = 1
+    a = local_thickness(data, Phase.BACKGROUND, ctx=gpu_ctx)
+    b = local_thickness(1 - data, Phase.FOREGROUND, ctx=gpu_ctx)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def check_stats(got, ref_map, scale):
+    n, s, ss, mx = O.exact_moment_sums(ref_map, scale)
+    mean, sd, mxr = O.stats_from_sums(n, s, ss, mx)
+    assert got.count == n
+    assert got.sum == s and got.sum_of_squares == ss
+    assert got.mean == mean and got.standard_deviation == sd and got.maximum == mxr
+    seq = O.nonzero_stats(ref_map, scale)
+    amp = (seq.mean / seq.sd) ** 2 if seq.sd > 0 else 1.0
+    assert abs(got.mean - seq.mean) <= seq_tol(n) * abs(seq.mean)
+    assert abs(got.maximum - seq.max) == 0.0
+    assert abs(got.standard_deviation - seq.sd) <= seq_tol(n, amp) * abs(seq.sd) + 1e-300
+
+
+def test_tbth_tbsp_plain_128(gpu_ctx):
+    sp = S.config_plain_128()
+    res = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx, return_maps=True)
+    for sel, got, gmap in ((True, res.thickness, res.thickness_map), (False, res.spacing, res.spacing_map)):
+        m = O.phase_inside(sp.bone, sp.roi, sel)
+        ref = O.local_thickness(m, O.FOREGROUND)
+        assert np.array_equal(gmap.view(np.uint32), ref.thickness.view(np.uint32))
+        check_stats(got, ref.thickness, sp.spacing_um)
+
+
+@pytest.mark.parametrize("seed", [21, 22])
+def test_tbth_tbsp_small_random_specimens(gpu_ctx, seed):
+    rng = np.random.default_rng(seed)
+    shape = tuple(int(v) for v in rng.integers(20, 70, size=3))
+    sp = S.make_specimen(shape, float(rng.uniform(1.5, 3)), float(rng.uniform(0.1, 0.4)), "cylinder",
+                         0.45 * min(shape[1], shape[2]), float(rng.uniform(5, 25)), seed)
+    res = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx, return_maps=True)
+    for sel, got, gmap in ((True, res.thickness, res.thickness_map), (False, res.spacing, res.spacing_map)):
+        m = O.phase_inside(sp.bone, sp.roi, sel)
+        ref = O.local_thickness(m, O.FOREGROUND)
+        assert np.array_equal(gmap.view(np.uint32), ref.thickness.view(np.uint32))
+        check_stats(got, ref.thickness, sp.spacing_um)
+
+
+def test_device_tensor_path(gpu_ctx):
+    import torch
+
+    sp = S.config_plain_128()
+    bone = torch.from_numpy(sp.bone).cuda()
+    roi = torch.from_numpy(sp.roi).cuda()
+    res_d = analyze_thickness(bone, roi, sp.spacing_um, ctx=gpu_ctx)
+    res_h = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx)
+    assert res_d.thickness.mean == res_h.thickness.mean
+    assert res_d.spacing.standard_deviation == res_h.spacing.standard_deviation
+    vol = torch.from_numpy(O.phase_inside(sp.bone, sp.roi, True)).cuda()
+    e = euclidean_distance_transform_squared(vol, ctx=gpu_ctx).cpu().numpy().view(np.uint32)
+    assert np.array_equal(e, O.edt_sq(vol.cpu().numpy()))
