@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Tb.Th + Tb.Sp throughput of the GB300 library (one JSON line on stdout).
+
+A step is one full pass of the hot path over one specimen: the exact squared
+EDT and the local thickness of ROI-clipped bone (Tb.Th) and of in-ROI marrow
+(Tb.Sp), reduced to mean / SD / max (metrics.rs:97-121).  The metric is input
+voxels (counted once per specimen) per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gpu|reference]
+
+--impl gpu (default): device-resident timing (``value``) with CUDA events on the
+launching stream, per-kernel event timing (roofline of the dominant kernel),
+an end-to-end leg through the host-pointer C ABI entry point with H2D/D2H in
+the timed region (``e2e``), the CPU oracle timed on a bounded sample
+(``cpu_baseline``), and nvidia-smi clock samples taken during the timed region.
+--impl reference: the reference algorithm's CPU implementation (the C++
+oracle, OpenMP over all host cores; the Rust reference cannot be built here)
+on bounded samples of the same workload.
+
+Multi-process (torchrun): every rank processes its own specimen (different
+seed, same shape) with no data exchange -- replicas, weak scaling; rank 0
+prints the line with the max time over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Gvoxel/s Tb.Th+Tb.Sp (EDT+local thickness), batched vs per-volume; p99 ms"
+UNIT = "Gvoxel/s"
+
+# Algorithmic bytes per voxel of each kernel family for one phase (reads +
+# writes a perfect kernel must make; bitmask words count 1/8 byte per voxel).
+ALGO_BYTES_PER_VOXEL = {
+    "edt_x": 2.0 + 4.0 + 0.125,        # bone + roi in, u32 out, selection bits out
+    "edt_y": 8.0,                      # u32 in, u32 out
+    "edt_z": 8.0,
+    "ridge": 4.0,                      # u32 distance map in (ridge records counted separately)
+    "fill": 4.0,                       # u32 squared-thickness map out
+    "cleanup_interior": 4.0 + 0.125,   # map in, bits out
+    "cleanup_final": 4.0 + 0.25,       # map in, two bitmasks in
+    "count_roi": 2.0,
+}
+EDT_FAMILIES = ("edt_x", "edt_y", "edt_z")
+
+WORKLOADS = {
+    "single512": dict(desc="512^3, sigma 5, BV/TV 0.15, cylinder ROI r240, 19.5 um", maker="config_single_512"),
+    "plain128": dict(desc="128^3, sigma 3, BV/TV 0.25, cylinder ROI r56, 10 um", maker="config_plain_128"),
+    "single1024": dict(desc="1024^3, sigma (4,4,8), BV/TV 0.30, sphere ROI r500, 8 um",
+                       maker="config_single_1024"),
+}
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gpu", "reference"), default="gpu")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="single512")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-slices", type=int, default=0,
+                    help="z-slab depth of the CPU sample (default: sized to ~10 s)")
+    return ap.parse_args(argv)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_specimen(workload: str, rank: int):
+    from bone_morphometry_gb300 import synthetic as S
+
+    maker = getattr(S, WORKLOADS[workload]["maker"])
+    base = maker.__defaults__[0]
+    return maker(seed=base + 7919 * rank)
+
+
+def measured_peak_gbs():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample_run(sp, slices: int, threads: int):
+    """Both phases of the oracle on a z-slab of the specimen; returns (voxels, seconds)."""
+    import numpy as np
+
+    import oracle as O
+
+    if threads:
+        O.set_threads(threads)
+    z0 = max(0, sp.bone.shape[0] // 2 - slices // 2)
+    bone = np.ascontiguousarray(sp.bone[z0:z0 + slices])
+    roi = np.ascontiguousarray(sp.roi[z0:z0 + slices])
+    t0 = time.perf_counter()
+    for sel in (True, False):
+        m = O.phase_inside(bone, roi, sel)
+        lt = O.local_thickness(m, O.FOREGROUND)
+        O.nonzero_stats(lt.thickness, sp.spacing_um)
+    return bone.size, time.perf_counter() - t0
+
+
+def default_slices(sp):
+    d, h, w = sp.bone.shape
+    # aim at ~10 s on a 16-core Grace host (~1.5 Mvoxel/s for both phases on this data)
+    target_vox = 15e6
+    return max(4, min(d, int(target_vox / (h * w))))
+
+
+def run_reference(args, rank, world):
+    """CPU implementation of the reference algorithm (oracle port), all host threads."""
+    import oracle as O
+
+    if rank != 0:
+        return 0
+    sp = make_specimen(args.workload, 0)
+    slices = args.cpu_sample_slices or default_slices(sp)
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    for _ in range(max(0, args.warmup)):
+        cpu_sample_run(sp, slices, threads)
+    times = []
+    vox = 0
+    for _ in range(args.steps):
+        vox, dt = cpu_sample_run(sp, slices, threads)
+        times.append(dt)
+    total = sum(times)
+    value = vox * len(times) / total / 1e9
+    d, h, w = sp.bone.shape
+    sample = "z-slab %dx%dx%d of the %s specimen, both phases" % (w, h, slices, args.workload)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u32/f32",
+        "data": "synthetic", "config": {"workload": "%s: %s" % (args.workload, WORKLOADS[args.workload]["desc"]),
+                                        "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the Rust reference cannot be built here (no cargo/rustc); the timed CPU path is the C++ "
+                "restatement of edt.rs / local_thickness.rs / metrics.rs with OpenMP in place of rayon",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from bone_morphometry_gb300 import Context, analyze_thickness
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    sp = make_specimen(args.workload, rank)
+    n_vox = sp.bone.size
+    ctx = Context(local)
+    stream = torch.cuda.current_stream()
+    bone = torch.from_numpy(sp.bone).cuda()
+    roi = torch.from_numpy(sp.roi).cuda()
+
+    for _ in range(max(3, args.warmup)):
+        ref_res = analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
+    torch.cuda.synchronize()
+
+    # -- device-resident leg ------------------------------------------------------------------
+    ctx.profile(True)
+    launches0 = ctx.launches
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            res = analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = ctx.launches - launches0
+    ktimes = ctx.kernel_times()
+    ctx.profile(False)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    assert res.thickness.mean == ref_res.thickness.mean and res.spacing.mean == ref_res.spacing.mean
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n_vox / (ms * 1e-3) / 1e9
+
+    # -- end-to-end leg through the host-pointer entry point (pinned host inputs) --------------
+    hb = torch.empty(sp.bone.shape, dtype=torch.uint8, pin_memory=True)
+    hr = torch.empty(sp.roi.shape, dtype=torch.uint8, pin_memory=True)
+    hb.numpy()[:] = sp.bone
+    hr.numpy()[:] = sp.roi
+    hbn, hrn = hb.numpy(), hr.numpy()
+    analyze_thickness(hbn, hrn, sp.spacing_um, ctx=ctx)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res_e = analyze_thickness(hbn, hrn, sp.spacing_um, ctx=ctx)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    assert res_e.thickness.mean == ref_res.thickness.mean
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n_vox / e2e_s / 1e9
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    # -- per-kernel times and roofline -------------------------------------------------------
+    total_kernel_ms = sum(v[1] for v in ktimes.values()) or 1.0
+    kernels = {}
+    for name, (nl, tms) in ktimes.items():
+        if nl == 0:
+            continue
+        kernels[name] = {"launches": nl, "ms_per_launch": tms / nl, "share": tms / total_kernel_ms}
+    peak, peak_src = measured_peak_gbs()
+    traffic = committed_traffic().get(args.workload, {})
+
+    def roof(name):
+        nl, tms = ktimes[name]
+        bpl = ALGO_BYTES_PER_VOXEL[name] * n_vox
+        achieved = bpl / (tms / nl * 1e-3) / 1e9
+        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic.get(name), "algorithmic_bytes": bpl,
+                "peak_source": peak_src}
+
+    dominant = max((k for k in ktimes if ktimes[k][0]), key=lambda k: ktimes[k][1])
+    edt_ms = sum(ktimes[k][1] for k in EDT_FAMILIES) / max(1, ktimes["edt_x"][0])
+    edt_bytes = sum(ALGO_BYTES_PER_VOXEL[k] for k in EDT_FAMILIES) * n_vox
+    edt_achieved = edt_bytes / (edt_ms * 1e-3) / 1e9
+
+    # -- CPU baseline (rank 0, N = 1 only) ------------------------------------------------------
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        slices = args.cpu_sample_slices or default_slices(sp)
+        vox, dt = cpu_sample_run(sp, slices, threads)
+        d, h, w = sp.bone.shape
+        cpu = {"value": vox / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "z-slab %dx%dx%d of the same specimen, both phases, %.1f s" % (w, h, slices, dt)}
+
+    d, h, w = sp.bone.shape
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8/u32/f32 (integer EDT and r^2, f32 map, exact f64 stats)",
+        "data": "synthetic (seeded Gaussian-smoothed noise, thresholded; no public dataset)",
+        "config": {"workload": "%s: %s" % (args.workload, WORKLOADS[args.workload]["desc"]),
+                   "shape_whd": [w, h, d], "voxels_per_specimen": n_vox, "phases": ["Tb.Th", "Tb.Sp"],
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs (%d MiB) and u32 maps (%d MiB each) larger than the 129 MB L2"
+                         % (2 * n_vox >> 20, 4 * n_vox >> 20)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n_vox,
+                "d2h_bytes_per_step": 2 * 104, "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches,
+        "roofline": roof(dominant),
+        "edt_roofline": {"bound": "hbm", "achieved": edt_achieved, "peak": peak, "unit": "GB/s",
+                         "frac": edt_achieved / peak, "algorithmic_bytes_per_phase": edt_bytes,
+                         "ms_per_phase": edt_ms, "peak_source": peak_src},
+        "kernels": kernels,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+        "result": {"TbTh_mean_um": res.thickness.mean, "TbTh_sd_um": res.thickness.standard_deviation,
+                   "TbSp_mean_um": res.spacing.mean, "TbSp_sd_um": res.spacing.standard_deviation},
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -41,6 +41,10 @@ class BoneMorphometryError(RuntimeError):
         self.status = status
 
 
+class BmKernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_uint64), ("total_ms", ctypes.c_double)]
+
+
 class BmStats(ctypes.Structure):
     _fields_ = [
         ("count", ctypes.c_uint64),
@@ -82,6 +86,8 @@ SIGNATURES = {
     "bm_tbth_tbsp_device": (_i, [_pctx, _u8p, _u8p, _sz, _sz, _sz, _d, _u, ctypes.POINTER(BmStats),
                                  ctypes.POINTER(BmStats), _vp, _vp, _vp]),
     "bm_ctx_launch_count": (ctypes.c_uint64, [_pctx]),
+    "bm_profile_enable": (_i, [_pctx, _i]),
+    "bm_profile_read": (_i, [_pctx, _vp, _sz, ctypes.POINTER(_sz)]),
 }
 
 _LIB = None
@@ -154,6 +160,17 @@ class Context:
     @property
     def launches(self) -> int:
         return int(self._lib.bm_ctx_launch_count(self.handle))
+
+    def profile(self, on: bool = True) -> None:
+        """Start (clearing totals) or stop CUDA-event timing of library kernels."""
+        self.call("bm_profile_enable", 1 if on else 0)
+
+    def kernel_times(self) -> dict:
+        """{family: (launches, total_ms)} of the kernels timed since profile(True)."""
+        arr = (BmKernelTime * 32)()
+        n = ctypes.c_size_t(0)
+        self.call("bm_profile_read", ctypes.cast(arr, ctypes.c_void_p), 32, ctypes.byref(n))
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(min(n.value, 32))}
 
     def call(self, name: str, *args) -> None:
         st = getattr(self._lib, name)(self.handle, *args)

@@ -72,6 +72,49 @@ void release(Buffer& b) {
   b.bytes = 0;
 }
 
+const char* const kFamilyName[KF_COUNT] = {"count_roi", "edt_x", "edt_y", "edt_z", "templates",
+                                            "ridge", "fill", "cleanup_interior", "cleanup_final"};
+
+cudaEvent_t pooled_event(bm_ctx* ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  check(ctx, cudaEventCreate(&e), "event create");
+  return e;
+}
+
+// Launch through `launch` (a callable returning cudaError_t); while profiling,
+// bracket it with events on the launching stream.
+template <class L>
+void timed(bm_ctx* ctx, int family, cudaStream_t s, const char* what, L&& launch) {
+  if (!ctx->profiling) {
+    check(ctx, launch(), what);
+    return;
+  }
+  cudaEvent_t a = pooled_event(ctx), b = pooled_event(ctx);
+  check(ctx, cudaEventRecord(a, s), "event record");
+  check(ctx, launch(), what);
+  check(ctx, cudaEventRecord(b, s), "event record");
+  ctx->prof.push_back(ProfRec{family, a, b});
+}
+
+void fold_profile(bm_ctx* ctx) {
+  for (const ProfRec& r : ctx->prof) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(r.stop) == cudaSuccess && cudaEventElapsedTime(&ms, r.start, r.stop) == cudaSuccess) {
+      ctx->prof_ms[r.family] += ms;
+      ctx->prof_n[r.family] += 1;
+    }
+    cudaGetLastError();
+    ctx->event_pool.push_back(r.start);
+    ctx->event_pool.push_back(r.stop);
+  }
+  ctx->prof.clear();
+}
+
 // volume.rs:12-34 plus the library's own limits (u32 linear ridge index, u32
 // squared distances whose search templates cannot overflow u32).
 Dims check_dims(bm_ctx* ctx, size_t w, size_t h, size_t d) {
@@ -110,7 +153,8 @@ void ensure_lut(bm_ctx* ctx, uint32_t rmax) {
           "template table copy");
     lo = ctx->lut_max + 1;
   }
-  check(ctx, launch_lut(static_cast<uint4*>(p), lo, target, ctx->stream, &ctx->launches), "template kernel");
+  timed(ctx, KF_TEMPLATES, ctx->stream, "template kernel",
+        [&] { return launch_lut(static_cast<uint4*>(p), lo, target, ctx->stream, &ctx->launches); });
   check(ctx, cudaStreamSynchronize(ctx->stream), "template kernel");
   release(ctx->lut);
   ctx->lut.ptr = p;
@@ -138,10 +182,13 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   Counters* ctr = static_cast<Counters*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
   check(ctx, cudaMemsetAsync(ctr, 0, sizeof(Counters), s), "memset");
 
-  check(ctx, launch_edt_x(d_a, d_b, mode, dm, A, selbits, ctr, s, &ctx->launches), "edt x pass");
-  check(ctx, launch_edt_line(1, A, B, dm, scratch, ctr, s, &ctx->launches), "edt y pass");
+  timed(ctx, KF_EDT_X, s, "edt x pass",
+        [&] { return launch_edt_x(d_a, d_b, mode, dm, A, selbits, ctr, s, &ctx->launches); });
+  timed(ctx, KF_EDT_Y, s, "edt y pass",
+        [&] { return launch_edt_line(1, A, B, dm, scratch, ctr, s, &ctx->launches); });
   uint32_t* E = d_edt ? d_edt : A;
-  check(ctx, launch_edt_line(2, B, E, dm, scratch, ctr, s, &ctx->launches), "edt z pass");
+  timed(ctx, KF_EDT_Z, s, "edt z pass",
+        [&] { return launch_edt_line(2, B, E, dm, scratch, ctr, s, &ctx->launches); });
 
   Counters hc;
   check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
@@ -160,15 +207,18 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   ensure_lut(ctx, hc.rmax);
   const uint4* lut = static_cast<const uint4*>(ctx->lut.ptr);
   uint2* ridges = static_cast<uint2*>(ensure(ctx, ctx->ridges, (res.selected + 1) * sizeof(uint2), "ridge list"));
-  check(ctx, launch_ridges(E, dm, lut, ridges, ctr, s, &ctx->launches), "ridge kernel");
+  timed(ctx, KF_RIDGE, s, "ridge kernel", [&] { return launch_ridges(E, dm, lut, ridges, ctr, s, &ctx->launches); });
   uint32_t* F = d_sq ? d_sq : B;
   check(ctx, cudaMemsetAsync(F, 0, N * 4, s), "memset");
-  check(ctx, launch_fill(ridges, ctr, res.selected, dm, F, s, &ctx->launches), "fill kernel");
+  timed(ctx, KF_FILL, s, "fill kernel",
+        [&] { return launch_fill(ridges, ctr, res.selected, dm, F, s, &ctx->launches); });
   uint32_t* posbits = static_cast<uint32_t*>(ensure(ctx, ctx->posbits, bits_bytes, "cleanup bits"));
-  check(ctx, launch_interior_bits(F, dm, posbits, s, &ctx->launches), "cleanup pass 1");
+  timed(ctx, KF_CLEAN_INTERIOR, s, "cleanup pass 1",
+        [&] { return launch_interior_bits(F, dm, posbits, s, &ctx->launches); });
   StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));
   check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
-  check(ctx, launch_final(F, posbits, selbits, dm, lut, scale, d_map, acc, s, &ctx->launches), "cleanup pass 2");
+  timed(ctx, KF_CLEAN_FINAL, s, "cleanup pass 2",
+        [&] { return launch_final(F, posbits, selbits, dm, lut, scale, d_map, acc, s, &ctx->launches); });
   check(ctx, cudaMemcpyAsync(&res.acc, acc, sizeof(StatsAccum), cudaMemcpyDeviceToHost, s), "stats readback");
   check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
   check(ctx, cudaStreamSynchronize(s), "local thickness");
@@ -279,9 +329,11 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
   unsigned long long* dcnt =
       static_cast<unsigned long long*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
   check(ctx, cudaMemsetAsync(dcnt, 0, 16, s), "memset");
-  count_roi_kernel<<<152 * 8, 256, 0, s>>>(d_bone, d_roi, N, dcnt);
-  ++ctx->launches;
-  check(ctx, cudaGetLastError(), "count kernel");
+  timed(ctx, KF_COUNT_ROI, s, "count kernel", [&] {
+    count_roi_kernel<<<152 * 8, 256, 0, s>>>(d_bone, d_roi, N, dcnt);
+    ++ctx->launches;
+    return cudaGetLastError();
+  });
   unsigned long long hc[2];
   check(ctx, cudaMemcpyAsync(hc, dcnt, 16, cudaMemcpyDeviceToHost, s), "count readback");
   check(ctx, cudaStreamSynchronize(s), "count kernel");
@@ -360,6 +412,11 @@ void bm_ctx_destroy(bm_ctx* ctx) {
                      &ctx->stack,   &ctx->fillmap, &ctx->selbits, &ctx->posbits, &ctx->ridges,
                      &ctx->counters, &ctx->accum,  &ctx->outmap,  &ctx->outmap2, &ctx->host_pinned};
     for (Buffer* b : all) release(*b);
+    for (const ProfRec& r : ctx->prof) {
+      cudaEventDestroy(r.start);
+      cudaEventDestroy(r.stop);
+    }
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
   }
   delete ctx;
@@ -397,6 +454,38 @@ size_t bm_last_error(const bm_ctx* ctx, char* buf, size_t len) {
 }
 
 uint64_t bm_ctx_launch_count(const bm_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int bm_profile_enable(bm_ctx* ctx, int on) {
+  return guarded(ctx, [&]() -> int {
+    fold_profile(ctx);
+    if (on) {
+      for (int i = 0; i < KF_COUNT; ++i) {
+        ctx->prof_ms[i] = 0.0;
+        ctx->prof_n[i] = 0;
+      }
+    }
+    ctx->profiling = on != 0;
+    return BM_OK;
+  });
+}
+
+int bm_profile_read(bm_ctx* ctx, bm_kernel_time* out, size_t cap, size_t* count) {
+  return guarded(ctx, [&]() -> int {
+    fold_profile(ctx);
+    size_t n = 0;
+    for (int i = 0; i < KF_COUNT; ++i) {
+      if (out && n < cap) {
+        std::memset(out[n].name, 0, sizeof out[n].name);
+        std::strncpy(out[n].name, kFamilyName[i], sizeof out[n].name - 1);
+        out[n].launches = ctx->prof_n[i];
+        out[n].total_ms = ctx->prof_ms[i];
+      }
+      ++n;
+    }
+    if (count) *count = n;
+    return BM_OK;
+  });
+}
 
 int bm_edt_sq_device(bm_ctx* ctx, const uint8_t* d_volume, size_t width, size_t height, size_t depth, int phase,
                      uint32_t* d_out, void* stream) {

@@ -6,6 +6,7 @@
 
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "bm.h"
 
@@ -54,6 +55,25 @@ struct Counters {  // device-side counters of one phase
   unsigned int status;  // nonzero: a bounded wait gave up / capacity exceeded
 };
 
+// Kernel families timed by the context's profiler (bm_profile_*).
+enum KernelFamily : int {
+  KF_COUNT_ROI = 0,
+  KF_EDT_X,
+  KF_EDT_Y,
+  KF_EDT_Z,
+  KF_TEMPLATES,
+  KF_RIDGE,
+  KF_FILL,
+  KF_CLEAN_INTERIOR,
+  KF_CLEAN_FINAL,
+  KF_COUNT
+};
+
+struct ProfRec {
+  int family;
+  cudaEvent_t start, stop;
+};
+
 }  // namespace bm
 
 struct bm_ctx {
@@ -79,4 +99,11 @@ struct bm_ctx {
   bm::Buffer outmap;           // f32 output staging
   bm::Buffer outmap2;
   bm::Buffer host_pinned;      // pinned staging for small readbacks
+
+  // profiler: CUDA events around every library launch while enabled
+  bool profiling = false;
+  std::vector<bm::ProfRec> prof;
+  std::vector<cudaEvent_t> event_pool;
+  double prof_ms[bm::KF_COUNT] = {};
+  unsigned long long prof_n[bm::KF_COUNT] = {};
 };

@@ -138,6 +138,20 @@ int bm_tbth_tbsp_device(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi
 /* Kernel launches issued by this context since creation (library kernels only). */
 uint64_t bm_ctx_launch_count(const bm_ctx* ctx);
 
+/* Per-kernel-family device time, measured with CUDA events recorded on the
+ * launching stream around every library kernel while profiling is enabled. */
+typedef struct bm_kernel_time {
+  char name[32];
+  uint64_t launches;
+  double total_ms;
+} bm_kernel_time;
+
+/* Enable (on != 0, clearing previous totals) or disable event timing. */
+int bm_profile_enable(bm_ctx* ctx, int on);
+/* Synchronise the context's pending work, fold recorded events into totals and
+ * copy up to cap families into out; *count receives the number of families. */
+int bm_profile_read(bm_ctx* ctx, bm_kernel_time* out, size_t cap, size_t* count);
+
 #ifdef __cplusplus
 }
 #endif
