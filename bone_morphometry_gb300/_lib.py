@@ -88,6 +88,7 @@ SIGNATURES = {
     "bm_ctx_launch_count": (ctypes.c_uint64, [_pctx]),
     "bm_profile_enable": (_i, [_pctx, _i]),
     "bm_profile_read": (_i, [_pctx, _vp, _sz, ctypes.POINTER(_sz)]),
+    "bm_edt_sq_device_noalloc": (_i, [_u8p, _sz, _sz, _sz, _i, _vp, _vp]),
 }
 
 _LIB = None

@@ -360,6 +360,12 @@ uint8_t* stage_input(bm_ctx* ctx, Buffer& b, const uint8_t* host, size_t n, cuda
 
 }  // namespace
 
+namespace bm {
+// Message returned by bm_last_error(NULL, ...) on this thread (used by the
+// entry points that take no context).
+void set_thread_error(const char* msg) { g_create_error = msg; }
+}  // namespace bm
+
 extern "C" {
 
 int bm_ctx_create(int device, bm_ctx** out) {

@@ -90,7 +90,7 @@ const char* bm_status_string(int status);
 
 /* Copy the last error message of `ctx` into buf (NUL-terminated, truncated to
  * len); returns the full message length.  ctx may be NULL for errors raised
- * by bm_ctx_create. */
+ * by bm_ctx_create and bm_edt_sq_device_noalloc (per host thread). */
 size_t bm_last_error(const bm_ctx* ctx, char* buf, size_t len);
 
 /* Release every cached device buffer of the context (kept otherwise, grown on
@@ -134,6 +134,23 @@ int bm_tbth_tbsp_device(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi
                         size_t height, size_t depth, double spacing_um, unsigned flags,
                         bm_stats* thickness, bm_stats* spacing, float* d_thickness_map,
                         float* d_spacing_map, void* stream);
+
+/* The exact squared EDT of bm_edt_sq_device without any device allocation.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc (a fixed device-memory budget owned by their own allocator, a
+ * footprint that must not grow after start-up, an embedding whose allocator
+ * they do not control).  Takes no context; all scratch lives in one static
+ * device array of 32 MiB held by every GPU that loads the library until the
+ * process exits, so volumes of up to about 2.7 million voxels (128^3 fits)
+ * are accepted and larger ones rejected with BM_ERR_DIMS.  The first call on
+ * a device looks up the array's address (once per device, that device
+ * current): make it before any stream capture.  All calls share the array and
+ * leave their data in it (the counters that must start at zero are cleared on
+ * each call); calls that overlap on the GPU race and must be serialised by the
+ * caller.  stream NULL = the legacy default stream; the call returns after
+ * synchronising it.  Errors: bm_last_error(NULL, ...). */
+int bm_edt_sq_device_noalloc(const uint8_t* d_volume, size_t width, size_t height, size_t depth,
+                             int phase, uint32_t* d_out, void* stream);
 
 /* Kernel launches issued by this context since creation (library kernels only). */
 uint64_t bm_ctx_launch_count(const bm_ctx* ctx);
