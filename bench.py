@@ -48,6 +48,9 @@ ALGO_BYTES_PER_VOXEL = {
     "edt_z": 8.0,
     "ridge": 4.0,                      # u32 distance map in (ridge records counted separately)
     "fill": 4.0,                       # u32 squared-thickness map out
+    "fill_rank": 0.0,                  # per-r^2 tables only
+    "fill_bin": 0.0,                   # per-ridge work (ridge records in, bin entries out)
+    "templates": 0.0,
     "cleanup_interior": 4.0 + 0.125,   # map in, bits out
     "cleanup_final": 4.0 + 0.25,       # map in, two bitmasks in
     "count_roi": 2.0,
@@ -184,8 +187,8 @@ def cpu_sample_run(sp, slices: int, threads: int):
 
 def default_slices(sp):
     d, h, w = sp.bone.shape
-    # aim at ~10 s on a 16-core Grace host (~1.5 Mvoxel/s for both phases on this data)
-    target_vox = 15e6
+    # aim at ~10 s on a 16-core Grace host (~8 Mvoxel/s for both phases of the 512^3 data)
+    target_vox = 80e6
     return max(4, min(d, int(target_vox / (h * w))))
 
 
@@ -321,7 +324,8 @@ def run_gpu(args, rank, world, local):
                 "frac": achieved / peak, "traffic": traffic.get(name), "algorithmic_bytes": bpl,
                 "peak_source": peak_src}
 
-    dominant = max((k for k in ktimes if ktimes[k][0]), key=lambda k: ktimes[k][1])
+    dominant = max((k for k in ktimes if ktimes[k][0] and ALGO_BYTES_PER_VOXEL.get(k, 0) > 0),
+                   key=lambda k: ktimes[k][1])
     edt_ms = sum(ktimes[k][1] for k in EDT_FAMILIES) / max(1, ktimes["edt_x"][0])
     edt_bytes = sum(ALGO_BYTES_PER_VOXEL[k] for k in EDT_FAMILIES) * n_vox
     edt_achieved = edt_bytes / (edt_ms * 1e-3) / 1e9

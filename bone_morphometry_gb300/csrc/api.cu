@@ -72,8 +72,9 @@ void release(Buffer& b) {
   b.bytes = 0;
 }
 
-const char* const kFamilyName[KF_COUNT] = {"count_roi", "edt_x", "edt_y", "edt_z", "templates",
-                                            "ridge", "fill", "cleanup_interior", "cleanup_final"};
+const char* const kFamilyName[KF_COUNT] = {"count_roi", "edt_x",     "edt_y",           "edt_z",
+                                            "templates", "ridge",     "fill",            "fill_rank",
+                                            "fill_bin",  "cleanup_interior", "cleanup_final"};
 
 cudaEvent_t pooled_event(bm_ctx* ctx) {
   if (!ctx->event_pool.empty()) {
@@ -162,6 +163,95 @@ void ensure_lut(bm_ctx* ctx, uint32_t rmax) {
   ctx->lut_max = target;
 }
 
+void ensure_surf(bm_ctx* ctx, uint32_t rmax);
+
+// Sphere fill of one phase into F (u32 r^2 map): tile-owned fill, or the
+// per-ball atomic scatter when the (ball, tile) entry count would not fit u32.
+void fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsigned long long max_ridges,
+                uint32_t rmax, const uint32_t* occ, const uint32_t* selbits, uint32_t* F, cudaStream_t s) {
+  const size_t rwords = (size_t)rmax + 2;
+  uint32_t* rank = static_cast<uint32_t*>(ensure(ctx, ctx->rank, rwords * 4, "r2 ranks"));
+  uint32_t* rvals = static_cast<uint32_t*>(ensure(ctx, ctx->rvals, rwords * 4, "r2 values"));
+  FillInfo* info = static_cast<FillInfo*>(ensure(ctx, ctx->fillinfo, sizeof(FillInfo), "fill info"));
+  uint32_t* scratch = static_cast<uint32_t*>(ensure(ctx, ctx->scanscratch, scan_scratch_words((long long)rwords) * 4,
+                                                    "scan scratch"));
+  check(ctx, cudaMemsetAsync(info, 0, sizeof(FillInfo), s), "memset");
+  timed(ctx, KF_FILL_RANK, s, "rank kernel",
+        [&] { return launch_rank(occ, rank, rmax, rvals, info, scratch, s, &ctx->launches); });
+  FillInfo hi;
+  check(ctx, cudaMemcpyAsync(&hi, info, sizeof hi, cudaMemcpyDeviceToHost, s), "fill info readback");
+  check(ctx, cudaStreamSynchronize(s), "rank kernel");
+  const long long tiles = fill_tile_count(dm);
+  const long long nbins = tiles * (long long)hi.nR;
+  uint32_t* counts = static_cast<uint32_t*>(ensure(ctx, ctx->bincounts, ((size_t)nbins + 1) * 4, "bin counts"));
+  uint32_t* offsets = static_cast<uint32_t*>(ensure(ctx, ctx->binoffsets, ((size_t)nbins + 1) * 4, "bin offsets"));
+  scratch = static_cast<uint32_t*>(ensure(ctx, ctx->scanscratch, scan_scratch_words(nbins + 1) * 4, "scan scratch"));
+  check(ctx, cudaMemsetAsync(counts, 0, ((size_t)nbins + 1) * 4, s), "memset");
+  if (hi.nR > 0) {
+    timed(ctx, KF_FILL_BIN, s, "bin count kernel", [&] {
+      return launch_bin(true, ridges, ctr, max_ridges, rank, info, dm, counts, nullptr, nullptr, s, &ctx->launches);
+    });
+  }
+  timed(ctx, KF_FILL_BIN, s, "bin scan",
+        [&] { return launch_scan(counts, offsets, nbins + 1, scratch, s, &ctx->launches); });
+  check(ctx, cudaMemcpyAsync(&hi, info, sizeof hi, cudaMemcpyDeviceToHost, s), "fill info readback");
+  check(ctx, cudaStreamSynchronize(s), "bin kernels");
+  if (hi.total_entries >= 0xFFFFFFFFull || rmax > kSurfMaxR2) {
+    check(ctx, cudaMemsetAsync(F, 0, (size_t)dm.n() * 4, s), "memset");
+    timed(ctx, KF_FILL, s, "fill kernel",
+          [&] { return launch_fill(ridges, ctr, max_ridges, dm, F, s, &ctx->launches); });
+    return;
+  }
+  uint32_t* entries = static_cast<uint32_t*>(
+      ensure(ctx, ctx->binentries, ((size_t)hi.total_entries + 1) * 4, "bin entries"));
+  if (hi.nR > 0) {
+    timed(ctx, KF_FILL_BIN, s, "bin scatter kernel", [&] {
+      return launch_bin(false, ridges, ctr, max_ridges, rank, info, dm, counts, offsets, entries, s, &ctx->launches);
+    });
+  }
+  ensure_surf(ctx, rmax);
+  timed(ctx, KF_FILL, s, "tile fill kernel", [&] {
+    return launch_tile_fill(entries, offsets, rvals, info, selbits, static_cast<const uint32_t*>(ctx->surf_off.ptr),
+                            static_cast<const uint32_t*>(ctx->surf_pts.ptr), dm, F, s, &ctx->launches);
+  });
+}
+
+// Lattice points of every sphere |d|^2 = r2 for r2 <= rmax, cached per context.
+void ensure_surf(bm_ctx* ctx, uint32_t rmax) {
+  if (ctx->surf_off.ptr && ctx->surf_max >= rmax) return;
+  uint32_t target = rmax < 1024 ? 1024 : rmax;
+  if (ctx->surf_off.ptr && target < ctx->surf_max * 2u) target = ctx->surf_max * 2u;
+  if (target > kSurfMaxR2) target = kSurfMaxR2 > rmax ? kSurfMaxR2 : rmax;
+  cudaStream_t s = ctx->stream;
+  const long long n = (long long)target + 2;
+  Buffer cnt;
+  uint32_t* c = static_cast<uint32_t*>(ensure(ctx, cnt, (size_t)n * 4, "sphere table"));
+  uint32_t* off = nullptr;
+  try {
+    release(ctx->surf_off);
+    release(ctx->surf_pts);
+    ctx->surf_max = 0;
+    off = static_cast<uint32_t*>(ensure(ctx, ctx->surf_off, (size_t)n * 4, "sphere table"));
+    uint32_t* scratch = static_cast<uint32_t*>(ensure(ctx, ctx->scanscratch, scan_scratch_words(n) * 4, "scan"));
+    check(ctx, cudaMemsetAsync(c, 0, (size_t)n * 4, s), "memset");
+    check(ctx, launch_surf(true, 0, target, c, nullptr, nullptr, s, &ctx->launches), "sphere table");
+    check(ctx, launch_scan(c, off, n, scratch, s, &ctx->launches), "sphere table");
+    uint32_t total = 0;
+    check(ctx, cudaMemcpyAsync(&total, off + target + 1, 4, cudaMemcpyDeviceToHost, s), "sphere table");
+    check(ctx, cudaStreamSynchronize(s), "sphere table");
+    uint32_t* pts = static_cast<uint32_t*>(ensure(ctx, ctx->surf_pts, ((size_t)total + 1) * 4, "sphere table"));
+    check(ctx, launch_surf(false, 0, target, nullptr, off, pts, s, &ctx->launches), "sphere table");
+    check(ctx, cudaStreamSynchronize(s), "sphere table");
+  } catch (...) {
+    release(cnt);
+    release(ctx->surf_off);
+    release(ctx->surf_pts);
+    throw;
+  }
+  release(cnt);
+  ctx->surf_max = target;
+}
+
 struct PhaseResult {
   unsigned long long sites = 0, selected = 0, ridges = 0;
   uint32_t rmax = 0;
@@ -207,11 +297,13 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   ensure_lut(ctx, hc.rmax);
   const uint4* lut = static_cast<const uint4*>(ctx->lut.ptr);
   uint2* ridges = static_cast<uint2*>(ensure(ctx, ctx->ridges, (res.selected + 1) * sizeof(uint2), "ridge list"));
-  timed(ctx, KF_RIDGE, s, "ridge kernel", [&] { return launch_ridges(E, dm, lut, ridges, ctr, s, &ctx->launches); });
+  const size_t rwords = (size_t)hc.rmax + 2;
+  uint32_t* occ = static_cast<uint32_t*>(ensure(ctx, ctx->occ, rwords * 4, "r2 flags"));
+  check(ctx, cudaMemsetAsync(occ, 0, rwords * 4, s), "memset");
+  timed(ctx, KF_RIDGE, s, "ridge kernel",
+        [&] { return launch_ridges(E, dm, lut, ridges, ctr, occ, s, &ctx->launches); });
   uint32_t* F = d_sq ? d_sq : B;
-  check(ctx, cudaMemsetAsync(F, 0, N * 4, s), "memset");
-  timed(ctx, KF_FILL, s, "fill kernel",
-        [&] { return launch_fill(ridges, ctr, res.selected, dm, F, s, &ctx->launches); });
+  fill_phase(ctx, dm, ridges, ctr, res.selected, hc.rmax, occ, selbits, F, s);
   uint32_t* posbits = static_cast<uint32_t*>(ensure(ctx, ctx->posbits, bits_bytes, "cleanup bits"));
   timed(ctx, KF_CLEAN_INTERIOR, s, "cleanup pass 1",
         [&] { return launch_interior_bits(F, dm, posbits, s, &ctx->launches); });
@@ -401,8 +493,10 @@ int bm_ctx_create(int device, bm_ctx** out) {
 int bm_ctx_trim(bm_ctx* ctx) {
   return guarded(ctx, [&]() -> int {
     cudaStreamSynchronize(ctx->stream);
-    Buffer* all[] = {&ctx->in_a, &ctx->in_b, &ctx->dist, &ctx->dist2, &ctx->stack, &ctx->fillmap, &ctx->selbits,
-                     &ctx->posbits, &ctx->ridges, &ctx->accum, &ctx->outmap, &ctx->outmap2};
+    Buffer* all[] = {&ctx->in_a,  &ctx->in_b,      &ctx->dist,       &ctx->dist2,      &ctx->stack,
+                     &ctx->fillmap, &ctx->selbits,  &ctx->posbits,   &ctx->ridges,     &ctx->accum,
+                     &ctx->outmap, &ctx->outmap2,  &ctx->occ,       &ctx->rank,       &ctx->rvals,
+                     &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch};
     for (Buffer* b : all) release(*b);
     return BM_OK;
   });
@@ -414,15 +508,19 @@ void bm_ctx_destroy(bm_ctx* ctx) {
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    Buffer* all[] = {&ctx->lut,     &ctx->in_a,   &ctx->in_b,     &ctx->dist,    &ctx->dist2,
-                     &ctx->stack,   &ctx->fillmap, &ctx->selbits, &ctx->posbits, &ctx->ridges,
-                     &ctx->counters, &ctx->accum,  &ctx->outmap,  &ctx->outmap2, &ctx->host_pinned};
+    Buffer* all[] = {&ctx->lut,      &ctx->in_a,      &ctx->in_b,       &ctx->dist,     &ctx->dist2,
+                     &ctx->stack,    &ctx->fillmap,   &ctx->selbits,    &ctx->posbits,  &ctx->ridges,
+                     &ctx->counters, &ctx->accum,     &ctx->outmap,     &ctx->outmap2,  &ctx->host_pinned,
+                     &ctx->occ,      &ctx->rank,      &ctx->rvals,      &ctx->fillinfo, &ctx->bincounts,
+                     &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch};
     for (Buffer* b : all) release(*b);
     for (const ProfRec& r : ctx->prof) {
       cudaEventDestroy(r.start);
       cudaEventDestroy(r.stop);
     }
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    release(ctx->surf_off);
+    release(ctx->surf_pts);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
   }
   delete ctx;

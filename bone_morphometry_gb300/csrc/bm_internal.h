@@ -41,6 +41,22 @@ struct StatsAccum {
   unsigned int pad;
 };
 
+// Tile of the tile-owned sphere fill (x, y, z voxels).
+constexpr int kFillTX = 32;
+constexpr int kFillTY = 32;
+constexpr int kFillTZ = 16;
+
+// Largest r^2 whose sphere lattice points the tile fill tabulates (radius 256);
+// volumes with larger distances use the per-ball atomic fill.
+constexpr uint32_t kSurfMaxR2 = 65536;
+
+// Device-side sizes of one phase's fill binning.
+struct FillInfo {
+  uint32_t nR;                         // distinct ridge r^2 values
+  uint32_t pad;
+  unsigned long long total_entries;    // (ball, tile) pairs
+};
+
 // Device scratch owned by a context, grown on demand and reused across calls.
 struct Buffer {
   void* ptr = nullptr;
@@ -64,6 +80,8 @@ enum KernelFamily : int {
   KF_TEMPLATES,
   KF_RIDGE,
   KF_FILL,
+  KF_FILL_RANK,
+  KF_FILL_BIN,
   KF_CLEAN_INTERIOR,
   KF_CLEAN_FINAL,
   KF_COUNT
@@ -99,6 +117,12 @@ struct bm_ctx {
   bm::Buffer outmap;           // f32 output staging
   bm::Buffer outmap2;
   bm::Buffer host_pinned;      // pinned staging for small readbacks
+  bm::Buffer occ, rank, rvals; // per-r^2 flags, ranks, rank -> r^2
+  bm::Buffer fillinfo;         // bm::FillInfo
+  bm::Buffer bincounts, binoffsets, binentries, scanscratch;
+  // cached sphere lattice-point table for r2 in [0, surf_max]
+  bm::Buffer surf_off, surf_pts;
+  uint32_t surf_max = 0;
 
   // profiler: CUDA events around every library launch while enabled
   bool profiling = false;

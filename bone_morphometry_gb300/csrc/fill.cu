@@ -1,0 +1,565 @@
+// Tile-owned sphere fill (local_thickness.rs:169-202) for sm_103a.
+//
+// The reference paints every voxel of every ridge ball with an atomic max:
+// sum over ridges of |ball| operations (~7e10 for a 512^3 marrow phase, where
+// every voxel is covered ~500 times).  Here the output volume is cut into
+// 32x32x16 tiles, each owned by one CTA that paints its tile in shared memory.
+// The balls that reach a tile are visited in strictly descending r^2 (a
+// counting sort by (tile, r^2 rank)); the final value of a voxel is the r^2 of
+// the first -- largest -- ball that covers it, so a per-row bitmask of
+// still-unpainted voxels lets every later ball skip whatever is already
+// decided.  Balls of equal r^2 paint the same value and run concurrently; a
+// barrier separates consecutive r^2 groups.  The result is the reference's
+// max-of-balls map bit for bit, with ~one shared-memory store per voxel plus
+// one mask test per (ball, row) instead of one global atomic per (ball, voxel).
+//
+// Pipeline (one phase):
+//   ridge_kernel       -> ridge records + occ[r2] flags
+//   scan(occ)          -> rank_desc[r2] (0 = largest r2 present), rvals[rank]
+//   bin_kernel<COUNT>  -> counts[tile * nR + rank]   (tiles the ball's box touches
+//                          and the ball reaches)
+//   scan(counts)       -> offsets
+//   bin_kernel<SCATTER>-> entries[offset..] = ball centre (linear index)
+//   tile_fill_kernel   -> u32 r^2 map
+#include "kernels.h"
+
+namespace bm {
+
+namespace {
+
+// floor(sqrt(v)) for v < 2^30: the correctly rounded single-precision root is
+// within one of the answer, so one correction step each way makes it exact.
+__device__ __forceinline__ uint32_t isqrt_u32(uint32_t v) {
+  uint32_t r = (uint32_t)sqrtf((float)v);
+  r -= (r * r > v) ? 1u : 0u;
+  r += ((r + 1) * (r + 1) <= v) ? 1u : 0u;
+  return r;
+}
+
+__device__ __forceinline__ uint32_t csqrt_u32(uint32_t v) {
+  const uint32_t f = isqrt_u32(v);
+  return f * f == v ? f : f + 1;
+}
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr long long kScanTile = kScanThreads * kScanItems;
+
+// Exclusive scan of one 4096-element tile; writes the tile total to sums.
+__global__ void __launch_bounds__(kScanThreads)
+scan_tile_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, long long n, uint32_t* __restrict__ sums) {
+  __shared__ uint32_t wsum[32];
+  const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t t = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < n) ? in[base + k] : 0u;
+    t += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = wsum[lane];
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += u;
+    }
+    wsum[lane] = wi - w;  // exclusive warp offsets
+    if (lane == 31) sums[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  uint32_t run = wsum[warp] + inc - t;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+}
+
+__global__ void scan_add_kernel(uint32_t* __restrict__ out, long long n, const uint32_t* __restrict__ tile_offsets) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] += tile_offsets[i / kScanTile];
+}
+
+// occ[0..rmax+1] flags (occ[rmax+1] = 0) -> ascending exclusive scan in
+// rank_desc (so rank_desc[rmax+1] = nR, never rewritten) -> rank_desc[r2] =
+// descending rank of every r2 present, rvals[rank] = r2, info->nR.
+__global__ void rank_finalize_kernel(const uint32_t* __restrict__ occ, uint32_t* __restrict__ rank_desc, uint32_t rmax,
+                                     uint32_t* __restrict__ rvals, FillInfo* __restrict__ info) {
+  const uint32_t nR = rank_desc[rmax + 1];
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r <= (long long)rmax;
+       r += (long long)gridDim.x * blockDim.x) {
+    if (occ[r]) {
+      const uint32_t rk = nR - 1u - rank_desc[r];
+      rank_desc[r] = rk;
+      rvals[rk] = (uint32_t)r;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) info->nR = nR;
+}
+
+struct Geom {
+  int ntx, nty, ntz;
+  long long ntiles;
+};
+
+__device__ __forceinline__ void decode(uint32_t idx, const Dims& dm, int& x, int& y, int& z) {
+  const uint32_t sl = (uint32_t)dm.w * (uint32_t)dm.h;
+  z = (int)(idx / sl);
+  const uint32_t rem = idx - (uint32_t)z * sl;
+  y = (int)(rem / (uint32_t)dm.w);
+  x = (int)(rem - (uint32_t)y * (uint32_t)dm.w);
+}
+
+// One thread per ridge: every tile whose box the ball reaches (closest point of
+// the tile within r^2 of the centre).  COUNT: counts[bin]++; else: place the
+// centre at offsets[bin] + (--counts[bin]).
+template <bool COUNT>
+__global__ void __launch_bounds__(256)
+bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, const uint32_t* __restrict__ rank_desc,
+           FillInfo* info, Dims dm, Geom g, uint32_t* __restrict__ counts,
+           const uint32_t* __restrict__ offsets, uint32_t* __restrict__ entries) {
+  const unsigned long long nr = ctr->ridges;
+  const uint32_t nR = info->nR;
+  unsigned long long touched = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (long long)nr;
+       i += (long long)gridDim.x * blockDim.x) {
+    const uint2 rec = ridges[i];
+    const uint32_t R = rec.y;
+    int x, y, z;
+    decode(rec.x, dm, x, y, z);
+    const int rad = (int)csqrt_u32(R);
+    const uint32_t rank = rank_desc[R];
+    const int tx0 = max(x - rad, 0) / kFillTX, tx1 = min(x + rad, dm.w - 1) / kFillTX;
+    const int ty0 = max(y - rad, 0) / kFillTY, ty1 = min(y + rad, dm.h - 1) / kFillTY;
+    const int tz0 = max(z - rad, 0) / kFillTZ, tz1 = min(z + rad, dm.d - 1) / kFillTZ;
+    for (int tz = tz0; tz <= tz1; ++tz) {
+      const int bz0 = tz * kFillTZ, bz1 = bz0 + kFillTZ - 1;
+      const long long ddz = z < bz0 ? bz0 - z : (z > bz1 ? z - bz1 : 0);
+      for (int ty = ty0; ty <= ty1; ++ty) {
+        const int by0 = ty * kFillTY, by1 = by0 + kFillTY - 1;
+        const long long ddy = y < by0 ? by0 - y : (y > by1 ? y - by1 : 0);
+        const long long dyz = ddz * ddz + ddy * ddy;
+        if (dyz > (long long)R) continue;
+        for (int tx = tx0; tx <= tx1; ++tx) {
+          const int bx0 = tx * kFillTX, bx1 = bx0 + kFillTX - 1;
+          const long long ddx = x < bx0 ? bx0 - x : (x > bx1 ? x - bx1 : 0);
+          if (dyz + ddx * ddx > (long long)R) continue;
+          const long long tile = ((long long)tz * g.nty + ty) * g.ntx + tx;
+          const long long bin = tile * nR + rank;
+          if (COUNT) {
+            atomicAdd(&counts[bin], 1u);
+            ++touched;
+          } else {
+            const uint32_t k = atomicSub(&counts[bin], 1u) - 1u;
+            entries[offsets[bin] + k] = rec.x;
+          }
+        }
+      }
+    }
+  }
+  if (COUNT) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) touched += __shfl_xor_sync(0xffffffffu, touched, o);
+    if ((threadIdx.x & 31) == 0 && touched) atomicAdd(&info->total_entries, touched);
+  }
+}
+
+constexpr int kFillThreads = 256;
+constexpr int kFillWarps = kFillThreads / 32;
+constexpr int kRows = kFillTZ * kFillTY;  // 512 rows of 32 voxels per tile
+
+__device__ __forceinline__ uint32_t range_mask(int a, int b) {  // bits a..b, 0 <= a <= b <= 31
+  return (0xffffffffu >> (31 - b)) & (0xffffffffu << a);
+}
+
+// Selection word of row (z, y), word c of a row-padded bitmask; 0 outside the volume.
+__device__ __forceinline__ uint32_t sel_word(const uint32_t* __restrict__ selbits, const Dims& dm, int nw, int z, int y,
+                                             int c) {
+  if (z < 0 || z >= dm.d || y < 0 || y >= dm.h || c < 0 || c >= nw) return 0u;
+  return selbits[((long long)z * dm.h + y) * nw + c];
+}
+
+constexpr int kBinChunk = 1024;   // bins whose offsets / r^2 are staged in shared memory at a time
+constexpr int kEntWin = 2048;     // ball entries staged in shared memory at a time
+
+// Half-word index of voxel (row, x) in the u16 value array: pairs of x share a
+// 32-bit word; the word is XOR-swizzled by the row so that threads touching the
+// same x of different rows fall into different banks.
+__device__ __forceinline__ int vidx(int row, int x) {
+  return row * 32 + (((((x >> 1) ^ (row & 15)) << 1)) | (x & 1));
+}
+
+// One CTA per tile (32 x 32 x 16 voxels).  Shared memory:
+//   val  : u16 per voxel, 0 = unpainted, else 1 + rank of the r^2 painted
+//          (rank 0 = largest r^2 present);
+//   usel : per row (z, y), the selected voxels not yet painted;
+//   usit : per row, the sites a ball can still paint.  A ball centred on a
+//          selected voxel p has r^2 = squared distance to p's nearest site, so
+//          it covers a site only when the site lies exactly on its sphere, and
+//          such a site has a selected 26-neighbour (one step towards p): usit
+//          starts as the sites of the selection's 3x3x3 dilation;
+//   pln  : per plane z, the rows whose usel is not empty;
+//   boff / brv / nzb : the tile's bin offsets, bin r^2 and the list of
+//          non-empty bins for the current chunk of bins;
+//   ent  : a window of the tile's ball entries, decoded to tile-local
+//          coordinates (10 bits each, biased by 512).
+// Bins arrive largest r^2 first with a barrier between bins, so the first ball
+// to reach a voxel carries its final value and later balls skip decided
+// voxels.  Inside a bin the work is flattened over the CTA: (ball, sphere
+// point) pairs paint sites, (ball, plane) pairs walk the plane's open rows and
+// paint chord & usel.
+__global__ void __launch_bounds__(kFillThreads, 4)
+tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
+                 const uint32_t* __restrict__ rvals, const FillInfo* __restrict__ info,
+                 const uint32_t* __restrict__ selbits, const uint32_t* __restrict__ surf_off,
+                 const uint32_t* __restrict__ surf_pts, Dims dm, Geom g, uint32_t* __restrict__ fillmap) {
+  extern __shared__ uint32_t smem[];
+  uint16_t* val = reinterpret_cast<uint16_t*>(smem);       // kRows * 32 half-words
+  uint32_t* usel = smem + kRows * 16;                        // kRows
+  uint32_t* usit = usel + kRows;                             // kRows
+  uint32_t* pln = usit + kRows;                              // kFillTZ
+  uint32_t* boff = pln + kFillTZ;                            // kBinChunk + 1
+  uint32_t* brv = boff + kBinChunk + 1;                      // kBinChunk
+  uint32_t* nzb = brv + kBinChunk;                           // kBinChunk
+  uint32_t* ent = nzb + kBinChunk;                           // kEntWin
+  __shared__ uint32_t s_nnz, s_wlo, s_whi;
+  // ldiv[ny*33 + k] = (k / ny) | (k % ny) << 8 for row counts ny = 1..32 and k = 0..32
+  __shared__ uint16_t ldiv[33 * 33];
+  for (int i = threadIdx.x; i < 33 * 33; i += blockDim.x) {
+    const int ny = i / 33, k = i % 33;
+    ldiv[i] = ny ? (uint16_t)((k / ny) | ((k % ny) << 8)) : (uint16_t)0;
+  }
+  const uint32_t nR = info->nR;
+  const int nw = dm.nw();
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  for (long long tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x) {
+    const int tx = (int)(tile % g.ntx);
+    const int ty = (int)((tile / g.ntx) % g.nty);
+    const int tz = (int)(tile / ((long long)g.ntx * g.nty));
+    const int x0 = tx * kFillTX, y0 = ty * kFillTY, z0 = tz * kFillTZ;
+    const int vx = min(kFillTX, dm.w - x0), vy = min(kFillTY, dm.h - y0), vz = min(kFillTZ, dm.d - z0);
+    const uint32_t xmask = vx >= 32 ? 0xffffffffu : ((1u << vx) - 1u);
+    const uint32_t* off = offsets + tile * (long long)nR;
+    if (off[0] == off[nR]) {  // no ball reaches this tile: all zero
+      for (int r = warp; r < kRows; r += kFillWarps) {
+        const int zz = r / kFillTY, yy = r % kFillTY;
+        if (zz < vz && yy < vy && lane < vx)
+          fillmap[((long long)(z0 + zz) * dm.h + (y0 + yy)) * dm.w + x0 + lane] = 0u;
+      }
+      continue;
+    }
+    for (int i = tid; i < kRows * 16; i += kFillThreads) smem[i] = 0u;
+    if (tid < kFillTZ) pln[tid] = 0u;
+    if (tid == 0) {
+      s_wlo = 0u;
+      s_whi = 0u;
+    }
+    __syncthreads();
+    for (int r = tid; r < kRows; r += kFillThreads) {
+      const int zz = r / kFillTY, yy = r % kFillTY;
+      uint32_t own = 0u, dil = 0u;
+      if (zz < vz && yy < vy) {
+        const int z = z0 + zz, y = y0 + yy;
+        uint32_t c = 0u, lft = 0u, rgt = 0u;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy) {
+            c |= sel_word(selbits, dm, nw, z + dz, y + dy, tx);
+            lft |= sel_word(selbits, dm, nw, z + dz, y + dy, tx - 1);
+            rgt |= sel_word(selbits, dm, nw, z + dz, y + dy, tx + 1);
+          }
+        own = sel_word(selbits, dm, nw, z, y, tx) & xmask;
+        dil = (c | (c << 1) | (c >> 1) | (lft >> 31) | (rgt << 31)) & xmask;
+      }
+      usel[r] = own;
+      usit[r] = dil & ~own;
+      if (own) atomicOr(&pln[zz], 1u << yy);
+    }
+    for (uint32_t b0 = 0; b0 < nR; b0 += kBinChunk) {
+      const uint32_t nb = min((uint32_t)kBinChunk, nR - b0);
+      __syncthreads();
+      for (uint32_t i = tid; i <= nb; i += kFillThreads) boff[i] = off[b0 + i];
+      for (uint32_t i = tid; i < nb; i += kFillThreads) brv[i] = rvals[b0 + i];
+      if (tid == 0) s_nnz = 0u;
+      __syncthreads();
+      // compact the non-empty bins, preserving order (warp ballots + one atomic per warp)
+      for (uint32_t base = 0; base < nb; base += kFillThreads) {
+        const uint32_t i = base + tid;
+        const bool ne = i < nb && boff[i] != boff[i + 1];
+        const unsigned m = __ballot_sync(0xffffffffu, ne);
+        __shared__ uint32_t wcnt[kFillWarps];
+        if (lane == 0) wcnt[warp] = __popc(m);
+        __syncthreads();
+        uint32_t before = 0;
+        for (int w = 0; w < warp; ++w) before += wcnt[w];
+        if (ne) nzb[s_nnz + before + __popc(m & ((1u << lane) - 1u))] = i;
+        __syncthreads();
+        if (tid == 0) {
+          uint32_t t = 0;
+          for (int w = 0; w < kFillWarps; ++w) t += wcnt[w];
+          s_nnz += t;
+        }
+        __syncthreads();
+      }
+      const uint32_t nnz = s_nnz;
+      for (uint32_t k = 0; k < nnz; ++k) {
+        const uint32_t bl = nzb[k];
+        const uint32_t R = brv[bl];
+        const uint16_t tag = (uint16_t)(b0 + bl + 1u);
+        const int rad = (int)csqrt_u32(R);
+        const uint32_t p0 = surf_off[R], np = surf_off[R + 1] - p0;
+        const uint32_t e = boff[bl + 1];
+        for (uint32_t ss = boff[bl]; ss < e;) {
+          if (ss < s_wlo || ss >= s_whi) {  // reload the entry window at ss (uniform decision)
+            __syncthreads();
+            const uint32_t lo = ss, hi = min(ss + (uint32_t)kEntWin, off[nR]);
+            for (uint32_t i = lo + tid; i < hi; i += kFillThreads) {
+              int cx, cy, cz;
+              decode(entries[i], dm, cx, cy, cz);
+              ent[i - lo] = (uint32_t)(cx - x0 + 512) | ((uint32_t)(cy - y0 + 512) << 10) |
+                            ((uint32_t)(cz - z0 + 512) << 20);
+            }
+            if (tid == 0) {
+              s_wlo = lo;
+              s_whi = hi;
+            }
+            __syncthreads();
+          }
+          const uint32_t se = min(e, s_whi);
+          const uint32_t* eb = ent + (ss - s_wlo);
+          // one warp per ball
+          for (uint32_t bi = warp; bi < se - ss; bi += kFillWarps) {
+            const uint32_t c = eb[bi];
+            const int cx = (int)(c & 0x3ffu) - 512, cy = (int)((c >> 10) & 0x3ffu) - 512, cz = (int)(c >> 20) - 512;
+            // sites: lanes over the lattice points of the sphere
+            for (uint32_t p = lane; p < np; p += 32) {
+              const uint32_t pk = surf_pts[p0 + p];
+              const int sx = cx + ((int)(pk << 22) >> 22);
+              const int sy = cy + ((int)(pk << 12) >> 22);
+              const int sz = cz + ((int)(pk << 2) >> 22);
+              if ((unsigned)sx < (unsigned)vx && (unsigned)sy < (unsigned)vy && (unsigned)sz < (unsigned)vz) {
+                const int row = sz * kFillTY + sy;
+                const uint32_t bit = 1u << sx;
+                if (usit[row] & bit) {
+                  atomicAnd(&usit[row], ~bit);
+                  val[vidx(row, sx)] = tag;
+                }
+              }
+            }
+            // selected voxels: lanes walk the rows of the ball's box inside the tile
+            const int zlo = max(cz - rad, 0), zhi = min(cz + rad, vz - 1);
+            const int ylo = max(cy - rad, 0), yhi = min(cy + rad, vy - 1);
+            if (zlo > zhi || ylo > yhi) continue;
+            const int ny = yhi - ylo + 1;
+            const int nrows = (zhi - zlo + 1) * ny;
+            const uint32_t dv = ldiv[ny * 33 + lane], st = ldiv[ny * 33 + 32];
+            int zz = zlo + (int)(dv & 0xffu), yy = ylo + (int)(dv >> 8);
+            const int stepz = (int)(st & 0xffu), stepy = (int)(st >> 8);
+            for (int r = lane; r < nrows; r += 32) {
+              if ((pln[zz] >> yy) & 1u) {
+                const int dz = zz - cz, dy = yy - cy;
+                const uint32_t dyz = (uint32_t)(dz * dz + dy * dy);
+                if (dyz <= R) {
+                  const int row = zz * kFillTY + yy;
+                  const uint32_t m = usel[row];
+                  const int hx = (int)isqrt_u32(R - dyz);
+                  const int xa = max(cx - hx, 0), xb = min(cx + hx, vx - 1);
+                  if (m && xa <= xb) {
+                    uint32_t bits = m & range_mask(xa, xb);
+                    if (bits) {
+                      const uint32_t old = atomicAnd(&usel[row], ~bits);
+                      if ((old & ~bits) == 0u) atomicAnd(&pln[zz], ~(1u << yy));
+                      while (bits) {
+                        const int xx = __ffs(bits) - 1;
+                        val[vidx(row, xx)] = tag;
+                        bits &= bits - 1u;
+                      }
+                    }
+                  }
+                }
+              }
+              yy += stepy;
+              zz += stepz;
+              if (yy > yhi) {
+                yy -= ny;
+                ++zz;
+              }
+            }
+          }
+          ss = se;
+        }
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+    // write the tile: one 128-byte row per warp step, rank -> r^2
+    for (int r = warp; r < kRows; r += kFillWarps) {
+      const int zz = r / kFillTY, yy = r % kFillTY;
+      if (zz < vz && yy < vy && lane < vx) {
+        const uint32_t t = val[vidx(r, lane)];
+        fillmap[((long long)(z0 + zz) * dm.h + (y0 + yy)) * dm.w + x0 + lane] = t ? rvals[t - 1u] : 0u;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Lattice points of the sphere |d|^2 = r2: one warp per r2, lanes over dz.
+// COUNT: surf_cnt[r2] = number of points; else write them packed
+// (10-bit two's-complement dx | dy << 10 | dz << 20) from surf_off[r2] on.
+template <bool COUNT>
+__global__ void __launch_bounds__(256)
+surf_kernel(uint32_t lo, uint32_t hi, uint32_t* __restrict__ surf_cnt, const uint32_t* __restrict__ surf_off,
+            uint32_t* __restrict__ surf_pts) {
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long rr = (long long)lo + wid; rr <= (long long)hi; rr += nwarps) {
+    const uint32_t R = (uint32_t)rr;
+    const int r = (int)isqrt_u32(R);
+    uint32_t mine = 0;
+    for (int dz = -r + lane; dz <= r; dz += 32) {
+      const uint32_t rz = R - (uint32_t)(dz * dz);
+      const int ry = (int)isqrt_u32(rz);
+      for (int dy = -ry; dy <= ry; ++dy) {
+        const uint32_t rx2 = rz - (uint32_t)(dy * dy);
+        const uint32_t k = isqrt_u32(rx2);
+        if (k * k == rx2) mine += k ? 2u : 1u;
+      }
+    }
+    if (COUNT) {
+      uint32_t cnt = mine;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      if (lane == 0) surf_cnt[R] = cnt;
+    } else {
+      uint32_t incl = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+      }
+      uint32_t pos = surf_off[R] + incl - mine;
+      for (int dz = -r + lane; dz <= r; dz += 32) {
+        const uint32_t rz = R - (uint32_t)(dz * dz);
+        const int ry = (int)isqrt_u32(rz);
+        for (int dy = -ry; dy <= ry; ++dy) {
+          const uint32_t rx2 = rz - (uint32_t)(dy * dy);
+          const uint32_t k = isqrt_u32(rx2);
+          if (k * k != rx2) continue;
+          const uint32_t yz = (((uint32_t)dy & 0x3ffu) << 10) | (((uint32_t)dz & 0x3ffu) << 20);
+          surf_pts[pos++] = (k & 0x3ffu) | yz;
+          if (k) surf_pts[pos++] = ((uint32_t)(-(int)k) & 0x3ffu) | yz;
+        }
+      }
+    }
+  }
+}
+
+Geom geom_of(Dims dm) {
+  Geom g;
+  g.ntx = (dm.w + kFillTX - 1) / kFillTX;
+  g.nty = (dm.h + kFillTY - 1) / kFillTY;
+  g.ntz = (dm.d + kFillTZ - 1) / kFillTZ;
+  g.ntiles = (long long)g.ntx * g.nty * g.ntz;
+  return g;
+}
+
+inline unsigned blocks_for(long long work, int per_block, long long cap) {
+  long long b = (work + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+long long fill_tile_count(Dims dm) { return geom_of(dm).ntiles; }
+
+size_t scan_scratch_words(long long n) {
+  size_t words = 0;
+  while (n > 1) {
+    n = (n + kScanTile - 1) / kScanTile;
+    words += (size_t)n + 1;
+  }
+  return words + 1;
+}
+
+cudaError_t launch_scan(const uint32_t* in, uint32_t* out, long long n, uint32_t* scratch, cudaStream_t s,
+                        unsigned long long* launches) {
+  if (n <= 0) return cudaSuccess;
+  const long long nb = (n + kScanTile - 1) / kScanTile;
+  uint32_t* sums = scratch;
+  scan_tile_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums);
+  ++*launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || nb == 1) return e;
+  e = launch_scan(sums, sums, nb, scratch + nb + 1, s, launches);
+  if (e != cudaSuccess) return e;
+  scan_add_kernel<<<blocks_for(n, 256, 152 * 64), 256, 0, s>>>(out, n, sums);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rank(const uint32_t* occ, uint32_t* rank_desc, uint32_t rmax, uint32_t* rvals, FillInfo* info,
+                        uint32_t* scan_scratch, cudaStream_t s, unsigned long long* launches) {
+  cudaError_t e = launch_scan(occ, rank_desc, (long long)rmax + 2, scan_scratch, s, launches);
+  if (e != cudaSuccess) return e;
+  rank_finalize_kernel<<<blocks_for((long long)rmax + 1, 256, 1024), 256, 0, s>>>(occ, rank_desc, rmax, rvals, info);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bin(bool count, const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
+                       const uint32_t* rank_desc, FillInfo* info, Dims dm, uint32_t* counts,
+                       const uint32_t* offsets, uint32_t* entries, cudaStream_t s, unsigned long long* launches) {
+  const Geom g = geom_of(dm);
+  const unsigned blocks = blocks_for((long long)max_ridges, 256, 152 * 32);
+  if (count)
+    bin_kernel<true><<<blocks, 256, 0, s>>>(ridges, ctr, rank_desc, info, dm, g, counts, offsets, entries);
+  else
+    bin_kernel<false><<<blocks, 256, 0, s>>>(ridges, ctr, rank_desc, info, dm, g, counts, offsets, entries);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_surf(bool count, uint32_t lo, uint32_t hi, uint32_t* surf_cnt, const uint32_t* surf_off,
+                        uint32_t* surf_pts, cudaStream_t s, unsigned long long* launches) {
+  if (hi < lo) return cudaSuccess;
+  const unsigned blocks = blocks_for((long long)hi - lo + 1, 8, 152 * 16);
+  if (count)
+    surf_kernel<true><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts);
+  else
+    surf_kernel<false><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
+                             const FillInfo* info, const uint32_t* selbits, const uint32_t* surf_off,
+                             const uint32_t* surf_pts, Dims dm, uint32_t* fillmap, cudaStream_t s,
+                             unsigned long long* launches) {
+  const Geom g = geom_of(dm);
+  const size_t smem =
+      (size_t)(kRows * 16 + 2 * kRows + kFillTZ + (kBinChunk + 1) + 2 * kBinChunk + kEntWin) * sizeof(uint32_t);
+  cudaError_t e = cudaFuncSetAttribute(tile_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const long long grid = g.ntiles < (1LL << 31) - 1 ? g.ntiles : (1LL << 31) - 1;
+  tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, info, selbits, surf_off,
+                                                               surf_pts, dm, g, fillmap);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+}  // namespace bm

@@ -23,9 +23,10 @@ cudaError_t launch_edt_line(int axis, const uint32_t* in, uint32_t* out, Dims dm
 // {scan_cube(1,0,0), scan_cube(1,1,0), scan_cube(1,1,1), f32 bits of 2*sqrt(r2)}.
 cudaError_t launch_lut(uint4* lut, uint32_t lo, uint32_t hi, cudaStream_t s, unsigned long long* launches);
 
-// Distance-ridge extraction: appends {linear index, r2} records.
+// Distance-ridge extraction: appends {linear index, r2} records and, when occ
+// is not null, sets occ[r2] = 1 for every ridge r2.
 cudaError_t launch_ridges(const uint32_t* dist, Dims dm, const uint4* lut, uint2* ridges,
-                          Counters* ctr, cudaStream_t s, unsigned long long* launches);
+                          Counters* ctr, uint32_t* occ, cudaStream_t s, unsigned long long* launches);
 
 // Sphere fill: atomic max of r2 over every voxel of each ridge ball (any phase).
 cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long long max_ridges, Dims dm,
@@ -39,5 +40,27 @@ cudaError_t launch_interior_bits(const uint32_t* fillmap, Dims dm, uint32_t* pos
 cudaError_t launch_final(const uint32_t* fillmap, const uint32_t* posbits, const uint32_t* selbits, Dims dm,
                          const uint4* lut, float scale, float* outmap, StatsAccum* acc, cudaStream_t s,
                          unsigned long long* launches);
+
+// Tile-owned fill (fill.cu).
+long long fill_tile_count(Dims dm);
+size_t scan_scratch_words(long long n);
+// Exclusive scan of n u32 values (out may alias in); scratch of scan_scratch_words(n).
+cudaError_t launch_scan(const uint32_t* in, uint32_t* out, long long n, uint32_t* scratch, cudaStream_t s,
+                        unsigned long long* launches);
+// occ[0..rmax+1] (occ[rmax+1] == 0) -> rank_desc / rvals / info->nR.
+cudaError_t launch_rank(const uint32_t* occ, uint32_t* rank_desc, uint32_t rmax, uint32_t* rvals, FillInfo* info,
+                        uint32_t* scan_scratch, cudaStream_t s, unsigned long long* launches);
+cudaError_t launch_bin(bool count, const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
+                       const uint32_t* rank_desc, FillInfo* info, Dims dm, uint32_t* counts,
+                       const uint32_t* offsets, uint32_t* entries, cudaStream_t s, unsigned long long* launches);
+// Sphere lattice-point table: count (surf_cnt[r2]) or fill (surf_pts from surf_off[r2]) for r2 in [lo, hi].
+cudaError_t launch_surf(bool count, uint32_t lo, uint32_t hi, uint32_t* surf_cnt, const uint32_t* surf_off,
+                        uint32_t* surf_pts, cudaStream_t s, unsigned long long* launches);
+// selbits: the phase's row-padded selection bitmask (edt_x output); surf_off /
+// surf_pts: the lattice-point table covering every ridge r2.
+cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
+                             const FillInfo* info, const uint32_t* selbits, const uint32_t* surf_off,
+                             const uint32_t* surf_pts, Dims dm, uint32_t* fillmap, cudaStream_t s,
+                             unsigned long long* launches);
 
 }  // namespace bm

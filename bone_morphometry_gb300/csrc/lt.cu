@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) lut_kernel(uint4* __restrict__ lut, uint3
 // local_thickness.rs:104-167 needs only the distance map.
 __global__ void __launch_bounds__(256)
 ridge_kernel(const uint32_t* __restrict__ dist, Dims dm, const uint4* __restrict__ lut, uint2* __restrict__ ridges,
-             Counters* __restrict__ ctr) {
+             Counters* __restrict__ ctr, uint32_t* __restrict__ occ) {
   const long long N = dm.n();
   const long long sl = (long long)dm.w * dm.h;
   const int lane = threadIdx.x & 31;
@@ -110,7 +110,10 @@ ridge_kernel(const uint32_t* __restrict__ dist, Dims dm, const uint4* __restrict
       const int leader = __ffs(m) - 1;
       if (lane == leader) slot = atomicAdd(&ctr->ridges, (unsigned long long)__popc(m));
       slot = __shfl_sync(0xffffffffu, slot, leader);
-      if (ridge) ridges[slot + __popc(m & ((1u << lane) - 1u))] = make_uint2((uint32_t)idx, R);
+      if (ridge) {
+        ridges[slot + __popc(m & ((1u << lane) - 1u))] = make_uint2((uint32_t)idx, R);
+        if (occ && occ[R] == 0u) occ[R] = 1u;  // read first: most ridges share few r2 values
+      }
     }
   }
 }
@@ -317,8 +320,8 @@ cudaError_t launch_lut(uint4* lut, uint32_t lo, uint32_t hi, cudaStream_t s, uns
 }
 
 cudaError_t launch_ridges(const uint32_t* dist, Dims dm, const uint4* lut, uint2* ridges, Counters* ctr,
-                          cudaStream_t s, unsigned long long* launches) {
-  ridge_kernel<<<grid_for(dm.n(), 256, 152 * 32), 256, 0, s>>>(dist, dm, lut, ridges, ctr);
+                          uint32_t* occ, cudaStream_t s, unsigned long long* launches) {
+  ridge_kernel<<<grid_for(dm.n(), 256, 152 * 32), 256, 0, s>>>(dist, dm, lut, ridges, ctr, occ);
   ++*launches;
   return cudaGetLastError();
 }

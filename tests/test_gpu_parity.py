@@ -120,6 +120,17 @@ def test_local_thickness_bitwise(gpu_ctx, kind, args, phase):
     assert np.array_equal(got.view(np.uint32), ref.thickness.view(np.uint32))
 
 
+def test_local_thickness_huge_balls(gpu_ctx):
+    # one site in a corner: r^2 up to ~3000, balls spanning many fill tiles
+    vol = np.ones((24, 30, 36), np.uint8)
+    vol[0, 0, 0] = 0
+    vol[23, 5, 30] = 0
+    ref = O.local_thickness(vol, O.FOREGROUND)
+    got, sq = local_thickness(vol, Phase.FOREGROUND, ctx=gpu_ctx, return_squared=True)
+    assert np.array_equal(sq, ref.propagated)
+    assert np.array_equal(got.view(np.uint32), ref.thickness.view(np.uint32))
+
+
 def test_isolated_voxel_has_diameter_two(gpu_ctx):
     # local_thickness.rs:364-374
     vol = np.zeros((3, 3, 3), np.uint8)
