@@ -274,11 +274,13 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
 
   timed(ctx, KF_EDT_X, s, "edt x pass",
         [&] { return launch_edt_x(d_a, d_b, mode, dm, A, selbits, ctr, s, &ctx->launches); });
+  const size_t redo_bytes = (size_t)dm.w * (dm.h > dm.d ? dm.h : dm.d);
+  uint8_t* redo = static_cast<uint8_t*>(ensure(ctx, ctx->redo, redo_bytes, "line flags"));
   timed(ctx, KF_EDT_Y, s, "edt y pass",
-        [&] { return launch_edt_line(1, A, B, dm, scratch, ctr, s, &ctx->launches); });
+        [&] { return launch_edt_window(1, A, B, dm, scratch, redo, ctr, s, &ctx->launches); });
   uint32_t* E = d_edt ? d_edt : A;
   timed(ctx, KF_EDT_Z, s, "edt z pass",
-        [&] { return launch_edt_line(2, B, E, dm, scratch, ctr, s, &ctx->launches); });
+        [&] { return launch_edt_window(2, B, E, dm, scratch, redo, ctr, s, &ctx->launches); });
 
   Counters hc;
   check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
@@ -496,7 +498,7 @@ int bm_ctx_trim(bm_ctx* ctx) {
     Buffer* all[] = {&ctx->in_a,  &ctx->in_b,      &ctx->dist,       &ctx->dist2,      &ctx->stack,
                      &ctx->fillmap, &ctx->selbits,  &ctx->posbits,   &ctx->ridges,     &ctx->accum,
                      &ctx->outmap, &ctx->outmap2,  &ctx->occ,       &ctx->rank,       &ctx->rvals,
-                     &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch};
+                     &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo};
     for (Buffer* b : all) release(*b);
     return BM_OK;
   });
@@ -512,7 +514,7 @@ void bm_ctx_destroy(bm_ctx* ctx) {
                      &ctx->stack,    &ctx->fillmap,   &ctx->selbits,    &ctx->posbits,  &ctx->ridges,
                      &ctx->counters, &ctx->accum,     &ctx->outmap,     &ctx->outmap2,  &ctx->host_pinned,
                      &ctx->occ,      &ctx->rank,      &ctx->rvals,      &ctx->fillinfo, &ctx->bincounts,
-                     &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch};
+                     &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo};
     for (Buffer* b : all) release(*b);
     for (const ProfRec& r : ctx->prof) {
       cudaEventDestroy(r.start);

@@ -122,6 +122,7 @@ struct bm_ctx {
   bm::Buffer bincounts, binoffsets, binentries, scanscratch;
   // cached sphere lattice-point table for r2 in [0, surf_max]
   bm::Buffer surf_off, surf_pts;
+  bm::Buffer redo;             // per-line flags of the windowed EDT passes
   uint32_t surf_max = 0;
 
   // profiler: CUDA events around every library launch while enabled

@@ -128,10 +128,10 @@ edt_x_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, Dims 
 __global__ void __launch_bounds__(256)
 edt_line_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int n, long long stride, int w,
                 long long outer, long long nlines, uint32_t* __restrict__ spos, uint32_t* __restrict__ sf,
-                Counters* __restrict__ ctr, int track_max) {
+                Counters* __restrict__ ctr, int track_max, const uint8_t* __restrict__ only) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t localmax = 0;
-  if (t < nlines) {
+  if (t < nlines && (only == nullptr || only[t])) {
     const long long base = (t / w) * outer + (t % w);
     int k = -1;
     long long p1 = 0, F1 = 0;  // stack top
@@ -194,6 +194,99 @@ edt_line_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) localmax = max(localmax, __shfl_xor_sync(0xffffffffu, localmax, o));
     if ((threadIdx.x & 31) == 0 && localmax) atomicMax(&ctr->rmax, localmax);
+  }
+}
+
+// Windowed y / z pass.  d(q) = min_p (q - p)^2 + f(p), and p = q already gives
+// f(q), so only |q - p| <= isqrt(f(q) - 1) can improve it: every output is an
+// exact minimum over a window whose width is bounded by its own input value.
+// A CTA owns 32 consecutive x of one line-row and kWinTL consecutive outputs
+// along the axis; it stages those inputs in shared memory as 128-byte rows,
+// then a halo on each side as wide as the largest window it needs (at most
+// kWinHalo).  Each lane scans outwards from its output and stops once dp^2
+// reaches the best value found.  Lines with an output whose window exceeds the
+// halo (or that has no site at all, f = kInfSq) are marked in `redo`; the
+// lower-envelope kernel recomputes exactly those lines afterwards.
+constexpr int kWinTL = 128;
+constexpr int kWinHalo = 64;
+constexpr int kWinThreads = 256;
+constexpr int kWinWarps = kWinThreads / 32;
+
+__global__ void __launch_bounds__(kWinThreads)
+edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int n, long long stride, int w,
+                  long long outer_stride, int nxt, int nchunk, uint8_t* __restrict__ redo, Counters* __restrict__ ctr,
+                  int track_max) {
+  __shared__ uint32_t buf[(kWinTL + 2 * kWinHalo) * 32];
+  __shared__ uint32_t s_need;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long bid = blockIdx.x;
+  const int xt = (int)(bid % nxt);
+  const int chunk = (int)((bid / nxt) % nchunk);
+  const long long orow = bid / ((long long)nxt * nchunk);
+  const int x = xt * 32 + lane;
+  const bool xin = x < w;
+  const long long base = orow * outer_stride + x;
+  const int q0 = chunk * kWinTL;
+  if (threadIdx.x == 0) s_need = 0u;
+  __syncthreads();
+  // centre rows
+  uint32_t need = 0;
+  for (int i = warp; i < kWinTL; i += kWinWarps) {
+    const int q = q0 + i;
+    uint32_t f = kInfSq;
+    if (xin && q < n) {
+      f = in[base + (long long)q * stride];
+      const uint32_t nd = (f == 0u) ? 0u : (f == kInfSq ? 0xffffu : (uint32_t)sqrtf((float)(f - 1u)) + 1u);
+      need = max(need, nd);
+    }
+    buf[(kWinHalo + i) * 32 + lane] = f;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
+  if (lane == 0) atomicMax(&s_need, need);
+  __syncthreads();
+  const int halo = (int)min(s_need, (uint32_t)kWinHalo);
+  for (int i = warp; i < halo; i += kWinWarps) {
+    const int ql = q0 - 1 - i, qr = q0 + kWinTL + i;
+    buf[(kWinHalo - 1 - i) * 32 + lane] = (xin && ql >= 0) ? in[base + (long long)ql * stride] : kInfSq;
+    buf[(kWinHalo + kWinTL + i) * 32 + lane] = (xin && qr < n) ? in[base + (long long)qr * stride] : kInfSq;
+  }
+  __syncthreads();
+  uint32_t localmax = 0;
+  bool bad = false;
+  for (int i = warp; i < kWinTL; i += kWinWarps) {
+    const int q = q0 + i;
+    if (!xin || q >= n) continue;
+    const uint32_t* col = buf + (kWinHalo + i) * 32 + lane;
+    uint32_t best = col[0];
+    if (best == 0u) {
+      out[base + (long long)q * stride] = 0u;
+      continue;
+    }
+    // every p with |q - p| < dp has been tried once dp^2 >= best; if the scan
+    // would have to pass the staged halo first, the line is redone exactly
+    bool done = true;
+    for (int dp = 1; (uint32_t)(dp * dp) < best; ++dp) {
+      if (dp > halo) {
+        done = false;
+        break;
+      }
+      const uint32_t a = col[-dp * 32], b = col[dp * 32];
+      const uint32_t c = min(a, b);
+      if (c != kInfSq) best = min(best, c + (uint32_t)(dp * dp));
+    }
+    if (!done) {
+      bad = true;
+      continue;
+    }
+    out[base + (long long)q * stride] = best;
+    localmax = max(localmax, best);
+  }
+  if (bad) redo[orow * (long long)w + x] = 1u;
+  if (track_max) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) localmax = max(localmax, __shfl_xor_sync(0xffffffffu, localmax, o));
+    if (lane == 0 && localmax) atomicMax(&ctr->rmax, localmax);
   }
 }
 
@@ -267,7 +360,44 @@ cudaError_t launch_edt_line(int axis, const uint32_t* in, uint32_t* out, Dims dm
   uint32_t* sf = spos + (size_t)nlines * n;
   const long long blocks = (nlines + 255) / 256;
   edt_line_kernel<<<(unsigned)blocks, 256, 0, s>>>(in, out, n, stride, dm.w, outer, nlines, spos, sf, ctr,
-                                                   axis == 2 ? 1 : 0);
+                                                   axis == 2 ? 1 : 0, nullptr);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_edt_window(int axis, const uint32_t* in, uint32_t* out, Dims dm, void* scratch, uint8_t* redo,
+                              Counters* ctr, cudaStream_t s, unsigned long long* launches) {
+  int n;
+  long long stride, outer, nlines, orows;
+  if (axis == 1) {
+    n = dm.h;
+    stride = dm.w;
+    outer = (long long)dm.w * dm.h;
+    nlines = (long long)dm.w * dm.d;
+    orows = dm.d;
+  } else {
+    n = dm.d;
+    stride = (long long)dm.w * dm.h;
+    outer = dm.w;
+    nlines = (long long)dm.w * dm.h;
+    orows = dm.h;
+  }
+  cudaError_t e = cudaMemsetAsync(redo, 0, (size_t)nlines, s);
+  if (e != cudaSuccess) return e;
+  const int nxt = (dm.w + 31) / 32;
+  const int nchunk = (n + kWinTL - 1) / kWinTL;
+  const long long blocks = (long long)nxt * nchunk * orows;
+  edt_window_kernel<<<(unsigned)blocks, kWinThreads, 0, s>>>(in, out, n, stride, dm.w, outer, nxt, nchunk, redo, ctr,
+                                                             axis == 2 ? 1 : 0);
+  ++*launches;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // exact lower envelope for the lines the window could not cover
+  uint32_t* spos = static_cast<uint32_t*>(scratch);
+  uint32_t* sf = spos + (size_t)nlines * n;
+  edt_line_kernel<<<(unsigned)((nlines + 255) / 256), 256, 0, s>>>(in, out, n, stride, dm.w,
+                                                                  axis == 1 ? (long long)dm.w * dm.h : dm.w, nlines,
+                                                                  spos, sf, ctr, axis == 2 ? 1 : 0, redo);
   ++*launches;
   return cudaGetLastError();
 }

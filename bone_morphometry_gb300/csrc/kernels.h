@@ -19,6 +19,11 @@ cudaError_t launch_edt_x(const uint8_t* a, const uint8_t* b, int mode, Dims dm, 
 cudaError_t launch_edt_line(int axis, const uint32_t* in, uint32_t* out, Dims dm, void* scratch,
                             Counters* ctr, cudaStream_t s, unsigned long long* launches);
 
+// Windowed y (axis 1) / z (axis 2) pass; lines it cannot bound are recomputed
+// by the lower-envelope kernel (redo: one byte per line, scratch as above).
+cudaError_t launch_edt_window(int axis, const uint32_t* in, uint32_t* out, Dims dm, void* scratch, uint8_t* redo,
+                              Counters* ctr, cudaStream_t s, unsigned long long* launches);
+
 // Search-template table entries lut[r2] for r2 in [lo, hi]:
 // {scan_cube(1,0,0), scan_cube(1,1,0), scan_cube(1,1,1), f32 bits of 2*sqrt(r2)}.
 cudaError_t launch_lut(uint4* lut, uint32_t lo, uint32_t hi, cudaStream_t s, unsigned long long* launches);

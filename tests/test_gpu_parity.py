@@ -38,7 +38,8 @@ def blob_volume(shape, sigma, frac, seed):
 EDT_CASES = [
     ((3, 3, 3), 0.5, 1), ((2, 2, 2), 0.5, 2), ((5, 7, 11), 0.3, 3), ((33, 31, 65), 0.9, 4),
     ((17, 129, 40), 0.97, 5), ((64, 64, 64), 0.5, 6), ((2, 300, 3), 0.99, 7), ((41, 2, 257), 0.8, 8),
-    ((16, 16, 1100), 0.995, 9),
+    ((16, 16, 1100), 0.995, 9), ((300, 200, 64), 0.999, 10), ((130, 140, 70), 0.98, 11),
+    ((257, 129, 33), 0.7, 12),
 ]
 
 
