@@ -306,13 +306,10 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
         [&] { return launch_ridges(E, dm, lut, ridges, ctr, occ, s, &ctx->launches); });
   uint32_t* F = d_sq ? d_sq : B;
   fill_phase(ctx, dm, ridges, ctr, res.selected, hc.rmax, occ, selbits, F, s);
-  uint32_t* posbits = static_cast<uint32_t*>(ensure(ctx, ctx->posbits, bits_bytes, "cleanup bits"));
-  timed(ctx, KF_CLEAN_INTERIOR, s, "cleanup pass 1",
-        [&] { return launch_interior_bits(F, dm, posbits, s, &ctx->launches); });
   StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));
   check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
-  timed(ctx, KF_CLEAN_FINAL, s, "cleanup pass 2",
-        [&] { return launch_final(F, posbits, selbits, dm, lut, scale, d_map, acc, s, &ctx->launches); });
+  timed(ctx, KF_CLEAN_FINAL, s, "cleanup",
+        [&] { return launch_cleanup(F, selbits, dm, lut, scale, d_map, acc, s, &ctx->launches); });
   check(ctx, cudaMemcpyAsync(&res.acc, acc, sizeof(StatsAccum), cudaMemcpyDeviceToHost, s), "stats readback");
   check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
   check(ctx, cudaStreamSynchronize(s), "local thickness");

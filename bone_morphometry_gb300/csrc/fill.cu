@@ -14,7 +14,7 @@
 // one mask test per (ball, row) instead of one global atomic per (ball, voxel).
 //
 // Pipeline (one phase):
-//   ridge_kernel       -> ridge records + occ[r2] flags
+//   ridge_tile_kernel  -> ridge records + occ[r2] flags
 //   scan(occ)          -> rank_desc[r2] (0 = largest r2 present), rvals[rank]
 //   bin_kernel<COUNT>  -> counts[tile * nR + rank]   (tiles the ball's box touches
 //                          and the ball reaches)

@@ -37,14 +37,9 @@ cudaError_t launch_ridges(const uint32_t* dist, Dims dm, const uint4* lut, uint2
 cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long long max_ridges, Dims dm,
                         uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
 
-// Surface cleanup pass 1 as a bitmask: nonzero voxel with no zero 26-neighbour.
-cudaError_t launch_interior_bits(const uint32_t* fillmap, Dims dm, uint32_t* posbits, cudaStream_t s,
-                                 unsigned long long* launches);
-
-// Cleanup pass 2, phase mask, optional f32 map, exact statistics.
-cudaError_t launch_final(const uint32_t* fillmap, const uint32_t* posbits, const uint32_t* selbits, Dims dm,
-                         const uint4* lut, float scale, float* outmap, StatsAccum* acc, cudaStream_t s,
-                         unsigned long long* launches);
+// Fused cleanup passes 1 and 2, phase mask, optional f32 map, exact statistics.
+cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const uint4* lut, float scale,
+                           float* outmap, StatsAccum* acc, cudaStream_t s, unsigned long long* launches);
 
 // Tile-owned fill (fill.cu).
 long long fill_tile_count(Dims dm);

@@ -60,64 +60,6 @@ __global__ void __launch_bounds__(256) lut_kernel(uint4* __restrict__ lut, uint3
   }
 }
 
-// Thread per voxel.  A voxel is selected exactly when its squared distance is
-// positive (non-selected voxels are sites, distance 0), so the ridge test of
-// local_thickness.rs:104-167 needs only the distance map.
-__global__ void __launch_bounds__(256)
-ridge_kernel(const uint32_t* __restrict__ dist, Dims dm, const uint4* __restrict__ lut, uint2* __restrict__ ridges,
-             Counters* __restrict__ ctr, uint32_t* __restrict__ occ) {
-  const long long N = dm.n();
-  const long long sl = (long long)dm.w * dm.h;
-  const int lane = threadIdx.x & 31;
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < N; base += (long long)gridDim.x * blockDim.x) {
-    const long long idx = base + threadIdx.x;
-    bool ridge = false;
-    uint32_t R = 0;
-    if (idx < N) {
-      R = dist[idx];
-      if (R > 0) {
-        const int z = (int)(idx / sl);
-        const long long rem = idx - (long long)z * sl;
-        const int y = (int)(rem / dm.w);
-        const int x = (int)(rem - (long long)y * dm.w);
-        const uint4 t = lut[R];
-        ridge = true;
-        for (int dz = -1; dz <= 1 && ridge; ++dz) {
-          const int nz = z + dz;
-          if (nz < 0 || nz >= dm.d) continue;
-          for (int dy = -1; dy <= 1 && ridge; ++dy) {
-            const int ny = y + dy;
-            if (ny < 0 || ny >= dm.h) continue;
-            const uint32_t* rowp = dist + ((long long)nz * dm.h + ny) * dm.w;
-            for (int dx = -1; dx <= 1; ++dx) {
-              if (dx == 0 && dy == 0 && dz == 0) continue;
-              const int nx = x + dx;
-              if (nx < 0 || nx >= dm.w) continue;
-              const int c = (dx != 0) + (dy != 0) + (dz != 0);
-              const uint32_t thr = c == 1 ? t.x : (c == 2 ? t.y : t.z);
-              if (rowp[nx] >= thr) {
-                ridge = false;
-                break;
-              }
-            }
-          }
-        }
-      }
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, ridge);
-    if (m) {
-      unsigned long long slot = 0;
-      const int leader = __ffs(m) - 1;
-      if (lane == leader) slot = atomicAdd(&ctr->ridges, (unsigned long long)__popc(m));
-      slot = __shfl_sync(0xffffffffu, slot, leader);
-      if (ridge) {
-        ridges[slot + __popc(m & ((1u << lane) - 1u))] = make_uint2((uint32_t)idx, R);
-        if (occ && occ[R] == 0u) occ[R] = 1u;  // read first: most ridges share few r2 values
-      }
-    }
-  }
-}
-
 // One warp per ridge ball; lanes take the (z, y) rows of the clipped box and
 // walk their chord |dx| <= isqrt(r2 - dy^2 - dz^2) (local_thickness.rs:172-202).
 __global__ void __launch_bounds__(256)
@@ -155,51 +97,6 @@ fill_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, 
   }
 }
 
-// Pass 1 of clean_up_surface_jaggies (local_thickness.rs:214-238) as a bit:
-// set for a nonzero voxel none of whose in-bounds 26-neighbours is zero (such a
-// voxel keeps its value; the others become -1).  One warp per 32-voxel word.
-__global__ void __launch_bounds__(256)
-interior_kernel(const uint32_t* __restrict__ fm, Dims dm, uint32_t* __restrict__ posbits) {
-  const int nw = dm.nw();
-  const long long words = (long long)nw * dm.h * dm.d;
-  const int lane = threadIdx.x & 31;
-  const long long wid0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long wi = wid0; wi < words; wi += nwarps) {
-    const long long row = wi / nw;
-    const int c = (int)(wi - row * nw);
-    const int y = (int)(row % dm.h);
-    const int z = (int)(row / dm.h);
-    const int x = c * 32 + lane;
-    bool pos = false;
-    if (x < dm.w) {
-      const long long idx = row * dm.w + x;
-      if (fm[idx] != 0u) {
-        pos = true;
-        for (int dz = -1; dz <= 1 && pos; ++dz) {
-          const int nz = z + dz;
-          if (nz < 0 || nz >= dm.d) continue;
-          for (int dy = -1; dy <= 1 && pos; ++dy) {
-            const int nyy = y + dy;
-            if (nyy < 0 || nyy >= dm.h) continue;
-            const uint32_t* rowp = fm + ((long long)nz * dm.h + nyy) * dm.w;
-            for (int dx = -1; dx <= 1; ++dx) {
-              const int nx = x + dx;
-              if (nx < 0 || nx >= dm.w) continue;
-              if (rowp[nx] == 0u) {
-                pos = false;
-                break;
-              }
-            }
-          }
-        }
-      }
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, pos);
-    if (lane == 0) posbits[wi] = m;
-  }
-}
-
 // NEIGHBORS_26 of local_thickness.rs:285-312 (Fiji's visitation order), which
 // fixes the order of the f32 sum in pass 2.
 __constant__ signed char kN26[26][3] = {
@@ -208,97 +105,251 @@ __constant__ signed char kN26[26][3] = {
     {-1, -1, 0}, {-1, 1, 0}, {-1, 0, -1}, {1, 0, -1}, {1, 1, 1},   {1, -1, 1}, {-1, 1, 1},
     {-1, -1, 1}, {1, 1, -1}, {1, -1, -1}, {-1, 1, -1}, {-1, -1, -1}};
 
-__device__ __forceinline__ bool bit_at(const uint32_t* __restrict__ bits, int nw, long long row, int x) {
-  return (bits[row * nw + (x >> 5)] >> (x & 31)) & 1u;
-}
+// Fused surface cleanup (local_thickness.rs:210-281), phase mask (:31-43),
+// f32 calibration and exact moment sums (metrics.rs:215-226) on a tile of
+// 32 x 8 x 8 voxels.  The r^2 map is staged with a halo of 2 (out-of-volume
+// voxels hold kOob, which is neither zero nor interior -- look() returns -1
+// there).  Pass 1 ("nonzero and no zero 26-neighbour") is a 3x3x3 erosion of
+// the nonzero mask, done on 64-bit row masks (x, then y, then z); pass 2 sums
+// the diameters of interior neighbours in NEIGHBORS_26 order with IEEE f32
+// adds and one IEEE division, exactly as the reference.
+constexpr int kCTX = 32, kCTY = 8, kCTZ = 8;
+constexpr int kCH = 2;                       // halo
+constexpr int kCSX = kCTX + 2 * kCH;         // 36
+constexpr int kCSY = kCTY + 2 * kCH;         // 12
+constexpr int kCSZ = kCTZ + 2 * kCH;         // 12
+constexpr uint32_t kOob = 0xffffffffu;
+constexpr int kCleanThreads = 256;
 
-__device__ __forceinline__ void accum_value(StatsAccum* s, float v) {
-  const uint32_t b = __float_as_uint(v);
-  uint32_t e = b >> 23;
-  uint32_t m = b & 0x7fffffu;
-  if (e) m |= 0x800000u;
-  else e = 1;
-  const unsigned long long sq = (unsigned long long)m * m;
-  atomicAdd(&s->sum_m[e], (unsigned long long)m);
-  atomicAdd(&s->sq_hi[e], sq >> 24);
-  atomicAdd(&s->sq_lo[e], sq & 0xffffffull);
-}
-
-// Pass 2 (local_thickness.rs:243-277), the final abs (:279), the phase mask
-// (:31-43), the f32 calibration multiply and the exact moment sums of
-// nonzero_stats (metrics.rs:215-226).  One warp per 32-voxel word.
-__global__ void __launch_bounds__(256)
-final_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict__ posbits,
-             const uint32_t* __restrict__ selbits, Dims dm, const uint4* __restrict__ lut, float scale,
-             float* __restrict__ outmap, StatsAccum* __restrict__ acc) {
+__global__ void __launch_bounds__(kCleanThreads)
+cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict__ selbits, Dims dm,
+                    const uint4* __restrict__ lut, float scale, float* __restrict__ outmap,
+                    StatsAccum* __restrict__ acc, int ntx, int nty, int ntz) {
+  __shared__ uint32_t T[kCSZ * kCSY * kCSX];         // f32 diameter bits of the r^2 map
+  __shared__ unsigned long long nz[kCSZ * kCSY];     // bit x: T != 0 (or out of volume)
+  __shared__ unsigned long long inr[kCSZ * kCSY];    // bit x: interior (pass-1 value kept)
+  __shared__ unsigned long long own[kCSZ * kCSY];    // bit x: T != 0 inside the volume
   __shared__ StatsAccum sacc;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < 256; i += kCleanThreads) {
     sacc.sum_m[i] = 0;
     sacc.sq_hi[i] = 0;
     sacc.sq_lo[i] = 0;
   }
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     sacc.count = 0;
     sacc.max_bits = 0;
   }
-  __syncthreads();
   const int nw = dm.nw();
-  const long long words = (long long)nw * dm.h * dm.d;
-  const int lane = threadIdx.x & 31;
-  const long long wid0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   unsigned long long cnt = 0;
   uint32_t mx = 0;
-  for (long long wi = wid0; wi < words; wi += nwarps) {
-    const long long row = wi / nw;
-    const int c = (int)(wi - row * nw);
-    const int y = (int)(row % dm.h);
-    const int z = (int)(row / dm.h);
-    const int x = c * 32 + lane;
-    if (x >= dm.w) continue;
-    const long long idx = row * dm.w + x;
-    float val = 0.0f;
-    const bool sel = (selbits[wi] >> lane) & 1u;
-    if (sel) {
-      const uint32_t T = fm[idx];
-      if (T != 0u) {
-        const float own = __uint_as_float(lut[T].w);
-        if ((posbits[wi] >> lane) & 1u) {
-          val = own;
-        } else {
-          int count = 0;
-          float sum = 0.0f;
-          for (int k = 0; k < 26; ++k) {
-            const int nx = x + kN26[k][0], nyy = y + kN26[k][1], nz = z + kN26[k][2];
-            if (nx < 0 || nyy < 0 || nz < 0 || nx >= dm.w || nyy >= dm.h || nz >= dm.d) continue;
-            const long long nrow = (long long)nz * dm.h + nyy;
-            if (!bit_at(posbits, nw, nrow, nx)) continue;
-            sum = __fadd_rn(sum, __uint_as_float(lut[fm[nrow * dm.w + nx]].w));
-            ++count;
-          }
-          val = count > 0 ? __fdiv_rn(sum, (float)count) : own;
-        }
+  const long long ntiles = (long long)ntx * nty * ntz;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
+    const int x0 = tx * kCTX, y0 = ty * kCTY, z0 = tz * kCTZ;
+    __syncthreads();
+    // stage the r^2 map with halo 2: one row of 36 per warp step
+    for (int r = warp; r < kCSZ * kCSY; r += kCleanThreads / 32) {
+      const int z = z0 - kCH + r / kCSY, y = y0 - kCH + r % kCSY;
+      const bool rin = z >= 0 && z < dm.d && y >= 0 && y < dm.h;
+      const uint32_t* row = fm + ((long long)z * dm.h + y) * dm.w;
+      uint32_t* srow = T + r * kCSX;
+      int x = x0 - kCH + lane;
+      uint32_t v = (rin && x >= 0 && x < dm.w) ? row[x] : kOob;
+      // staged as the f32 diameter bits (2*sqrt(r^2)); 0 stays 0
+      srow[lane] = (v == 0u || v == kOob) ? 0u : lut[v].w;
+      unsigned b = __ballot_sync(0xffffffffu, v != 0u);
+      uint32_t v2 = kOob;
+      if (lane < kCSX - 32) {
+        x = x0 - kCH + 32 + lane;
+        v2 = (rin && x < dm.w) ? row[x] : kOob;
+        srow[32 + lane] = (v2 == 0u || v2 == kOob) ? 0u : lut[v2].w;
+      }
+      const unsigned b2 = __ballot_sync(0xffffffffu, lane < kCSX - 32 && v2 != 0u);
+      const unsigned o1 = __ballot_sync(0xffffffffu, v != 0u && v != kOob);
+      const unsigned o2 = __ballot_sync(0xffffffffu, lane < kCSX - 32 && v2 != 0u && v2 != kOob);
+      if (lane == 0) {
+        nz[r] = (unsigned long long)b | ((unsigned long long)b2 << 32);
+        own[r] = (unsigned long long)o1 | ((unsigned long long)o2 << 32);
       }
     }
-    if (outmap) outmap[idx] = val;
-    if (val > 0.0f) {
-      const float v = __fmul_rn(val, scale);
-      accum_value(&sacc, v);
-      ++cnt;
-      mx = max(mx, __float_as_uint(v));
+    __syncthreads();
+    // pass 1: erosion of nz over x, y, z for the halo-1 region (rows z,y in [1, kCS-2])
+    for (int r = tid; r < kCSZ * kCSY; r += kCleanThreads) {
+      const int zz = r / kCSY, yy = r % kCSY;
+      unsigned long long m = 0;
+      if (zz >= 1 && zz <= kCSZ - 2 && yy >= 1 && yy <= kCSY - 2) {
+        m = ~0ull;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy) {
+            const unsigned long long q = nz[(zz + dz) * kCSY + yy + dy];
+            m &= q & (q << 1) & (q >> 1);
+          }
+        // interior also needs the voxel itself nonzero and inside the volume
+        m &= own[r];
+      }
+      inr[r] = m;
+    }
+    __syncthreads();
+    // pass 2 + mask + stats, one output row (32 voxels) per warp step
+    for (int r = warp; r < kCTZ * kCTY; r += kCleanThreads / 32) {
+      const int oz = r / kCTY, oy = r % kCTY;
+      const int z = z0 + oz, y = y0 + oy, x = x0 + lane;
+      if (z >= dm.d || y >= dm.h) continue;
+      const int sz = oz + kCH, sy = oy + kCH, sx = lane + kCH;
+      float val = 0.0f;
+      const bool sel = x < dm.w && ((selbits[((long long)z * dm.h + y) * nw + tx] >> lane) & 1u);
+      if (sel) {
+        const uint32_t t = T[(sz * kCSY + sy) * kCSX + sx];
+        if (t != 0u) {
+          const float own = __uint_as_float(t);
+          if ((inr[sz * kCSY + sy] >> sx) & 1ull) {
+            val = own;
+          } else {
+            int count = 0;
+            float sum = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 26; ++k) {
+              const int nx = sx + kN26[k][0], ny = sy + kN26[k][1], nzz = sz + kN26[k][2];
+              if ((inr[nzz * kCSY + ny] >> nx) & 1ull) {
+                sum = __fadd_rn(sum, __uint_as_float(T[(nzz * kCSY + ny) * kCSX + nx]));
+                ++count;
+              }
+            }
+            val = count > 0 ? __fdiv_rn(sum, (float)count) : own;
+          }
+        }
+      }
+      if (outmap && x < dm.w) outmap[((long long)z * dm.h + y) * dm.w + x] = val;
+      const unsigned pos = __ballot_sync(0xffffffffu, val > 0.0f);
+      if (val > 0.0f) {
+        const float v = __fmul_rn(val, scale);
+        ++cnt;
+        mx = max(mx, __float_as_uint(v));
+        // lanes holding the same exponent add their mantissa sums in one step
+        const uint32_t bits = __float_as_uint(v);
+        uint32_t e = bits >> 23, m = bits & 0x7fffffu;
+        if (e) m |= 0x800000u;
+        else e = 1;
+        const unsigned long long sq = (unsigned long long)m * m;
+        const unsigned grp = __match_any_sync(pos, e);
+        const uint32_t s1 = __reduce_add_sync(grp, m);
+        const uint32_t sh = __reduce_add_sync(grp, (uint32_t)(sq >> 24));
+        const uint32_t sl = __reduce_add_sync(grp, (uint32_t)(sq & 0xffffffu));
+        if (lane == __ffs(grp) - 1) {
+          atomicAdd(&sacc.sum_m[e], (unsigned long long)s1);
+          atomicAdd(&sacc.sq_hi[e], (unsigned long long)sh);
+          atomicAdd(&sacc.sq_lo[e], (unsigned long long)sl);
+        }
+      }
     }
   }
   if (cnt) atomicAdd(&sacc.count, cnt);
   if (mx) atomicMax(&sacc.max_bits, mx);
   __syncthreads();
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+  for (int i = tid; i < 256; i += kCleanThreads) {
     if (sacc.sum_m[i]) atomicAdd(&acc->sum_m[i], sacc.sum_m[i]);
     if (sacc.sq_hi[i]) atomicAdd(&acc->sq_hi[i], sacc.sq_hi[i]);
     if (sacc.sq_lo[i]) atomicAdd(&acc->sq_lo[i], sacc.sq_lo[i]);
   }
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     if (sacc.count) atomicAdd(&acc->count, sacc.count);
     if (sacc.max_bits) atomicMax(&acc->max_bits, sacc.max_bits);
+  }
+}
+
+// Distance ridge (local_thickness.rs:104-167) on 32 x 8 x 8 tiles with the
+// distance map staged with a halo of 1 (out-of-volume neighbours are skipped,
+// as in the reference's bounds checks).  A selected voxel (d > 0) is a ridge
+// unless some 26-neighbour's d reaches the search template of its own r^2
+// (offset class = number of nonzero components).
+constexpr int kRTX = 32, kRTY = 8, kRTZ = 8;
+constexpr int kRSX = kRTX + 2, kRSY = kRTY + 2, kRSZ = kRTZ + 2;
+
+__global__ void __launch_bounds__(256)
+ridge_tile_kernel(const uint32_t* __restrict__ dist, Dims dm, const uint4* __restrict__ lut,
+                  uint2* __restrict__ ridges, Counters* __restrict__ ctr, uint32_t* __restrict__ occ, int ntx,
+                  int nty, int ntz) {
+  __shared__ uint32_t D[kRSZ * kRSY * kRSX];
+  __shared__ uint32_t s_wcnt[8];
+  __shared__ unsigned long long s_base;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long ntiles = (long long)ntx * nty * ntz;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
+    const int x0 = tx * kRTX, y0 = ty * kRTY, z0 = tz * kRTZ;
+    __syncthreads();
+    for (int r = warp; r < kRSZ * kRSY; r += 8) {
+      const int z = z0 - 1 + r / kRSY, y = y0 - 1 + r % kRSY;
+      const bool rin = z >= 0 && z < dm.d && y >= 0 && y < dm.h;
+      const uint32_t* row = dist + ((long long)z * dm.h + y) * dm.w;
+      uint32_t* srow = D + r * kRSX;
+      int x = x0 - 1 + lane;
+      srow[lane] = (rin && x >= 0 && x < dm.w) ? row[x] : 0u;
+      if (lane < 2) {
+        x = x0 + 31 + lane;
+        srow[32 + lane] = (rin && x < dm.w) ? row[x] : 0u;
+      }
+    }
+    __syncthreads();
+    // ridge masks of this warp's 8 rows, then one global slot reservation per tile
+    unsigned mk[kRTZ * kRTY / 8];
+    int wcount = 0;
+#pragma unroll
+    for (int k = 0; k < kRTZ * kRTY / 8; ++k) {
+      const int r = warp + 8 * k;
+      const int oz = r / kRTY, oy = r % kRTY;
+      const int z = z0 + oz, y = y0 + oy, x = x0 + lane;
+      bool ridge = false;
+      if (z < dm.d && y < dm.h && x < dm.w) {
+        const int sx = lane + 1, sy = oy + 1, sz = oz + 1;
+        const uint32_t R = D[(sz * kRSY + sy) * kRSX + sx];
+        if (R > 0u) {
+          const uint4 t = lut[R];
+          ridge = true;
+          // neighbours outside the volume hold 0 and never reach a template (>= 4)
+#pragma unroll
+          for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+              for (int dx = -1; dx <= 1; ++dx) {
+                if (dx == 0 && dy == 0 && dz == 0) continue;
+                const int c = (dx != 0) + (dy != 0) + (dz != 0);
+                const uint32_t thr = c == 1 ? t.x : (c == 2 ? t.y : t.z);
+                if (D[((sz + dz) * kRSY + sy + dy) * kRSX + sx + dx] >= thr) ridge = false;
+              }
+        }
+      }
+      mk[k] = __ballot_sync(0xffffffffu, ridge);
+      wcount += __popc(mk[k]);
+    }
+    if (lane == 0) s_wcnt[warp] = (uint32_t)wcount;
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t tot = 0;
+      for (int w = 0; w < 8; ++w) {
+        const uint32_t c = s_wcnt[w];
+        s_wcnt[w] = tot;
+        tot += c;
+      }
+      s_base = tot ? atomicAdd(&ctr->ridges, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    unsigned long long slot = s_base + s_wcnt[warp];
+#pragma unroll
+    for (int k = 0; k < kRTZ * kRTY / 8; ++k) {
+      const unsigned m = mk[k];
+      if ((m >> lane) & 1u) {
+        const int r = warp + 8 * k;
+        const int oz = r / kRTY, oy = r % kRTY;
+        const int z = z0 + oz, y = y0 + oy, x = x0 + lane;
+        const uint32_t R = D[((oz + 1) * kRSY + oy + 1) * kRSX + lane + 1];
+        ridges[slot + __popc(m & ((1u << lane) - 1u))] = make_uint2((uint32_t)(((long long)z * dm.h + y) * dm.w + x), R);
+        if (occ && occ[R] == 0u) occ[R] = 1u;
+      }
+      slot += __popc(m);
+    }
   }
 }
 
@@ -321,7 +372,10 @@ cudaError_t launch_lut(uint4* lut, uint32_t lo, uint32_t hi, cudaStream_t s, uns
 
 cudaError_t launch_ridges(const uint32_t* dist, Dims dm, const uint4* lut, uint2* ridges, Counters* ctr,
                           uint32_t* occ, cudaStream_t s, unsigned long long* launches) {
-  ridge_kernel<<<grid_for(dm.n(), 256, 152 * 32), 256, 0, s>>>(dist, dm, lut, ridges, ctr, occ);
+  const int ntx = (dm.w + kRTX - 1) / kRTX, nty = (dm.h + kRTY - 1) / kRTY, ntz = (dm.d + kRTZ - 1) / kRTZ;
+  const long long tiles = (long long)ntx * nty * ntz;
+  ridge_tile_kernel<<<(unsigned)(tiles < 152 * 8 ? tiles : 152 * 8), 256, 0, s>>>(dist, dm, lut, ridges, ctr, occ, ntx,
+                                                                                 nty, ntz);
   ++*launches;
   return cudaGetLastError();
 }
@@ -333,20 +387,12 @@ cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long 
   return cudaGetLastError();
 }
 
-cudaError_t launch_interior_bits(const uint32_t* fillmap, Dims dm, uint32_t* posbits, cudaStream_t s,
-                                 unsigned long long* launches) {
-  const long long words = (long long)dm.nw() * dm.h * dm.d;
-  interior_kernel<<<grid_for(words, 8, 152 * 32), 256, 0, s>>>(fillmap, dm, posbits);
-  ++*launches;
-  return cudaGetLastError();
-}
-
-cudaError_t launch_final(const uint32_t* fillmap, const uint32_t* posbits, const uint32_t* selbits, Dims dm,
-                         const uint4* lut, float scale, float* outmap, StatsAccum* acc, cudaStream_t s,
-                         unsigned long long* launches) {
-  const long long words = (long long)dm.nw() * dm.h * dm.d;
-  final_kernel<<<grid_for(words, 8, 152 * 16), 256, 0, s>>>(fillmap, posbits, selbits, dm, lut, scale, outmap,
-                                                            acc);
+cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const uint4* lut, float scale,
+                           float* outmap, StatsAccum* acc, cudaStream_t s, unsigned long long* launches) {
+  const int ntx = (dm.w + kCTX - 1) / kCTX, nty = (dm.h + kCTY - 1) / kCTY, ntz = (dm.d + kCTZ - 1) / kCTZ;
+  const long long tiles = (long long)ntx * nty * ntz;
+  const unsigned grid = (unsigned)(tiles < 152 * 8 ? tiles : 152 * 8);
+  cleanup_tile_kernel<<<grid, kCleanThreads, 0, s>>>(fillmap, selbits, dm, lut, scale, outmap, acc, ntx, nty, ntz);
   ++*launches;
   return cudaGetLastError();
 }
