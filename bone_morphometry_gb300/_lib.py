@@ -89,6 +89,8 @@ SIGNATURES = {
     "bm_profile_enable": (_i, [_pctx, _i]),
     "bm_profile_read": (_i, [_pctx, _vp, _sz, ctypes.POINTER(_sz)]),
     "bm_edt_sq_device_noalloc": (_i, [_u8p, _sz, _sz, _sz, _i, _vp, _vp]),
+    "bm_nonzero_stats": (_i, [_pctx, _vp, _sz, _d, _u, ctypes.POINTER(BmStats)]),
+    "bm_nonzero_stats_device": (_i, [_pctx, _vp, _sz, _d, _u, ctypes.POINTER(BmStats), _vp]),
 }
 
 _LIB = None

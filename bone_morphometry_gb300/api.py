@@ -212,6 +212,25 @@ class ThicknessMetrics:
     spacing_map: object = None
 
 
+def nonzero_stats(values, scale: float, include_quantiles: bool = False, ctx: Context | None = None
+                  ) -> DistributionStats:
+    """metrics.rs:204-269 on an f32 map (numpy array or CUDA float32 tensor)."""
+    ctx = ctx or default_context()
+    out = BmStats()
+    flags = BM_FLAG_QUANTILES if include_quantiles else 0
+    if _is_cuda_tensor(values):
+        import torch
+
+        if values.dtype != torch.float32 or not values.is_contiguous():
+            raise BoneMorphometryError(BM_ERR_INVALID, "expected a contiguous float32 tensor")
+        ctx.call("bm_nonzero_stats_device", ctypes.c_void_p(values.data_ptr()), values.numel(), float(scale), flags,
+                 ctypes.byref(out), _stream_ptr(values))
+    else:
+        v = np.ascontiguousarray(np.asarray(values, dtype=np.float32)).reshape(-1)
+        ctx.call("bm_nonzero_stats", _ptr(v), v.size, float(scale), flags, ctypes.byref(out))
+    return DistributionStats.from_c(out)
+
+
 def _flags(feature_mode) -> int:
     fm = FeatureMode(feature_mode) if not isinstance(feature_mode, FeatureMode) else feature_mode
     flags = 0

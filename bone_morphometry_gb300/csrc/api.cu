@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "exact_sum.h"
 #include "kernels.h"
@@ -74,7 +75,8 @@ void release(Buffer& b) {
 
 const char* const kFamilyName[KF_COUNT] = {"count_roi", "edt_x",     "edt_y",           "edt_z",
                                             "templates", "ridge",     "fill",            "fill_rank",
-                                            "fill_bin",  "cleanup_interior", "cleanup_final"};
+                                            "fill_bin",  "cleanup_interior", "cleanup_final",
+                                            "quantile"};
 
 cudaEvent_t pooled_event(bm_ctx* ctx) {
   if (!ctx->event_pool.empty()) {
@@ -344,6 +346,88 @@ int finish_stats(bm_ctx* ctx, const StatsAccum& a, bm_stats* out) {
   return BM_OK;
 }
 
+// Quantiles of the finite positive values of d_map (metrics.rs:242-298):
+// median, P10, P25, P75, P90 by numpy-linear interpolation of exact order
+// statistics, then (q as f32 * scale_f32) as f64; IQR = P75 - P25.
+void quantiles(bm_ctx* ctx, const float* d_map, long long n, unsigned long long count, double scale,
+               bm_stats* out, cudaStream_t s) {
+  static const double kQ[5] = {0.5, 0.1, 0.25, 0.75, 0.9};  // metrics.rs:247-251
+  unsigned long long ranks[10];
+  double frac[5];
+  for (int i = 0; i < 5; ++i) {
+    const double position = kQ[i] * (double)(count - 1);
+    const double lo = std::floor(position), hi = std::ceil(position);
+    ranks[2 * i] = (unsigned long long)lo;
+    ranks[2 * i + 1] = (unsigned long long)hi;
+    frac[i] = position - lo;
+  }
+  uint32_t* hist = static_cast<uint32_t*>(ensure(ctx, ctx->qhist, (size_t)17 * 65536 * 4, "quantile histograms"));
+  uint32_t* dtargets = static_cast<uint32_t*>(ensure(ctx, ctx->qtargets, 16 * 4, "quantile targets"));
+  check(ctx, cudaMemsetAsync(hist, 0, (size_t)65536 * 4, s), "memset");
+  timed(ctx, KF_QUANTILE, s, "quantile histogram", [&] { return launch_hist_hi(d_map, n, hist, s, &ctx->launches); });
+  std::vector<uint32_t> hh(65536);
+  check(ctx, cudaMemcpyAsync(hh.data(), hist, 65536 * 4, cudaMemcpyDeviceToHost, s), "histogram readback");
+  check(ctx, cudaStreamSynchronize(s), "quantile histogram");
+  // locate every rank's high-16 bin and its rank inside that bin
+  uint32_t tgt[10];
+  unsigned long long resid[10];
+  for (int r = 0; r < 10; ++r) {
+    unsigned long long cum = 0;
+    uint32_t b = 0;
+    for (; b < 65536; ++b) {
+      if (cum + hh[b] > ranks[r]) break;
+      cum += hh[b];
+    }
+    if (b == 65536) fail(ctx, BM_ERR_CUDA, "quantile rank %llu beyond %llu values", ranks[r], cum);
+    tgt[r] = b;
+    resid[r] = ranks[r] - cum;
+  }
+  uint32_t uniq[10];
+  int nu = 0;
+  int slot_of[10];
+  for (int r = 0; r < 10; ++r) {
+    int j = 0;
+    while (j < nu && uniq[j] != tgt[r]) ++j;
+    if (j == nu) uniq[nu++] = tgt[r];
+    slot_of[r] = j;
+  }
+  uint32_t* lo = hist + 65536;
+  check(ctx, cudaMemcpyAsync(dtargets, uniq, (size_t)nu * 4, cudaMemcpyHostToDevice, s), "targets upload");
+  check(ctx, cudaMemsetAsync(lo, 0, (size_t)nu * 65536 * 4, s), "memset");
+  timed(ctx, KF_QUANTILE, s, "quantile histogram",
+        [&] { return launch_hist_lo(d_map, n, dtargets, nu, lo, s, &ctx->launches); });
+  std::vector<uint32_t> hl((size_t)nu * 65536);
+  check(ctx, cudaMemcpyAsync(hl.data(), lo, hl.size() * 4, cudaMemcpyDeviceToHost, s), "histogram readback");
+  check(ctx, cudaStreamSynchronize(s), "quantile histogram");
+  double v[10];
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t* h = hl.data() + (size_t)slot_of[r] * 65536;
+    unsigned long long cum = 0;
+    uint32_t b = 0;
+    for (; b < 65536; ++b) {
+      if (cum + h[b] > resid[r]) break;
+      cum += h[b];
+    }
+    const uint32_t bits = (tgt[r] << 16) | b;
+    float f;
+    std::memcpy(&f, &bits, 4);
+    v[r] = (double)f;
+  }
+  const float sf = (float)scale;
+  double q[5];
+  for (int i = 0; i < 5; ++i) {
+    const double lv = v[2 * i], uv = v[2 * i + 1];
+    const double qv = lv + frac[i] * (uv - lv);  // metrics.rs:289
+    q[i] = (double)((float)qv * sf);             // metrics.rs:290
+  }
+  out->median = q[0];
+  out->percentile_10 = q[1];
+  out->percentile_25 = q[2];
+  out->percentile_75 = q[3];
+  out->percentile_90 = q[4];
+  out->interquartile_range = q[3] - q[2];
+}
+
 template <class F>
 int guarded(bm_ctx* ctx, F&& f) {
   if (!ctx) return BM_ERR_INVALID;
@@ -415,7 +499,6 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
          spacing);
   if (flags & ~(unsigned)(BM_FLAG_QUANTILES | BM_FLAG_BONEJ_ROI))
     fail(ctx, BM_ERR_INVALID, "unknown flags 0x%x", flags);
-  if (flags & BM_FLAG_QUANTILES) fail(ctx, BM_ERR_INVALID, "quantiles are not available in this build");
   const long long N = dm.n();
   unsigned long long* dcnt =
       static_cast<unsigned long long*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
@@ -435,12 +518,22 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
   if (hc[1] == hc[0]) fail(ctx, BM_ERR_NO_MARROW, "ROI contains no marrow voxels");
 
   const float scale = (float)spacing;  // metrics.rs:213
+  const bool want_q = (flags & BM_FLAG_QUANTILES) != 0;
+  float* qm = nullptr;
+  if (want_q && (!d_thmap || !d_spmap))
+    qm = static_cast<float*>(ensure(ctx, ctx->qmap, (size_t)N * 4, "quantile map"));
   PhaseResult rb, rm;
-  run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, d_thmap, nullptr, scale, s, rb);
+  float* mb = d_thmap ? d_thmap : qm;
+  run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, s, rb);
   int st = finish_stats(ctx, rb.acc, th);
   if (st) return st;
-  run_phase(ctx, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, d_spmap, nullptr, scale, s, rm);
-  return finish_stats(ctx, rm.acc, sp);
+  if (want_q && th) quantiles(ctx, mb, N, rb.acc.count, spacing, th, s);
+  float* mm = d_spmap ? d_spmap : qm;
+  run_phase(ctx, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, s, rm);
+  st = finish_stats(ctx, rm.acc, sp);
+  if (st) return st;
+  if (want_q && sp) quantiles(ctx, mm, N, rm.acc.count, spacing, sp, s);
+  return BM_OK;
 }
 
 uint8_t* stage_input(bm_ctx* ctx, Buffer& b, const uint8_t* host, size_t n, cudaStream_t s) {
@@ -495,7 +588,8 @@ int bm_ctx_trim(bm_ctx* ctx) {
     Buffer* all[] = {&ctx->in_a,  &ctx->in_b,      &ctx->dist,       &ctx->dist2,      &ctx->stack,
                      &ctx->fillmap, &ctx->selbits,  &ctx->posbits,   &ctx->ridges,     &ctx->accum,
                      &ctx->outmap, &ctx->outmap2,  &ctx->occ,       &ctx->rank,       &ctx->rvals,
-                     &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo};
+                     &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
+                     &ctx->qhist, &ctx->qtargets, &ctx->qmap};
     for (Buffer* b : all) release(*b);
     return BM_OK;
   });
@@ -511,7 +605,8 @@ void bm_ctx_destroy(bm_ctx* ctx) {
                      &ctx->stack,    &ctx->fillmap,   &ctx->selbits,    &ctx->posbits,  &ctx->ridges,
                      &ctx->counters, &ctx->accum,     &ctx->outmap,     &ctx->outmap2,  &ctx->host_pinned,
                      &ctx->occ,      &ctx->rank,      &ctx->rvals,      &ctx->fillinfo, &ctx->bincounts,
-                     &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo};
+                     &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
+                     &ctx->qhist,    &ctx->qtargets,  &ctx->qmap};
     for (Buffer* b : all) release(*b);
     for (const ProfRec& r : ctx->prof) {
       cudaEventDestroy(r.start);
@@ -643,6 +738,47 @@ int bm_local_thickness(bm_ctx* ctx, const uint8_t* volume, size_t width, size_t 
     if (squared_thickness)
       check(ctx, cudaMemcpyAsync(squared_thickness, d_sq, N * 4, cudaMemcpyDeviceToHost, s), "result download");
     check(ctx, cudaStreamSynchronize(s), "result download");
+    return BM_OK;
+  });
+}
+
+int bm_nonzero_stats_device(bm_ctx* ctx, const float* d_values, size_t n, double scale, unsigned flags,
+                            bm_stats* out, void* stream) {
+  return guarded(ctx, [&]() -> int {
+    if (!d_values || !out) fail(ctx, BM_ERR_INVALID, "null pointer");
+    if (flags & ~(unsigned)BM_FLAG_QUANTILES) fail(ctx, BM_ERR_INVALID, "unknown flags 0x%x", flags);
+    cudaStream_t s = pick_stream(ctx, stream);
+    StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));
+    check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
+    timed(ctx, KF_QUANTILE, s, "moments kernel",
+          [&] { return launch_moments(d_values, (long long)n, (float)scale, acc, s, &ctx->launches); });
+    StatsAccum ha;
+    check(ctx, cudaMemcpyAsync(&ha, acc, sizeof ha, cudaMemcpyDeviceToHost, s), "stats readback");
+    check(ctx, cudaStreamSynchronize(s), "moments kernel");
+    int st = finish_stats(ctx, ha, out);
+    if (st) return st;
+    if (flags & BM_FLAG_QUANTILES) quantiles(ctx, d_values, (long long)n, ha.count, scale, out, s);
+    return BM_OK;
+  });
+}
+
+int bm_nonzero_stats(bm_ctx* ctx, const float* values, size_t n, double scale, unsigned flags, bm_stats* out) {
+  return guarded(ctx, [&]() -> int {
+    if (!values || !out) fail(ctx, BM_ERR_INVALID, "null pointer");
+    if (flags & ~(unsigned)BM_FLAG_QUANTILES) fail(ctx, BM_ERR_INVALID, "unknown flags 0x%x", flags);
+    cudaStream_t s = ctx->stream;
+    float* d = static_cast<float*>(ensure(ctx, ctx->qmap, (n ? n : 1) * 4, "values"));
+    if (n) check(ctx, cudaMemcpyAsync(d, values, n * 4, cudaMemcpyHostToDevice, s), "values upload");
+    StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));
+    check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
+    timed(ctx, KF_QUANTILE, s, "moments kernel",
+          [&] { return launch_moments(d, (long long)n, (float)scale, acc, s, &ctx->launches); });
+    StatsAccum ha;
+    check(ctx, cudaMemcpyAsync(&ha, acc, sizeof ha, cudaMemcpyDeviceToHost, s), "stats readback");
+    check(ctx, cudaStreamSynchronize(s), "moments kernel");
+    int st = finish_stats(ctx, ha, out);
+    if (st) return st;
+    if (flags & BM_FLAG_QUANTILES) quantiles(ctx, d, (long long)n, ha.count, scale, out, s);
     return BM_OK;
   });
 }

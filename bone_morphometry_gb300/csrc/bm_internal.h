@@ -84,6 +84,7 @@ enum KernelFamily : int {
   KF_FILL_BIN,
   KF_CLEAN_INTERIOR,
   KF_CLEAN_FINAL,
+  KF_QUANTILE,
   KF_COUNT
 };
 
@@ -123,6 +124,7 @@ struct bm_ctx {
   // cached sphere lattice-point table for r2 in [0, surf_max]
   bm::Buffer surf_off, surf_pts;
   bm::Buffer redo;             // per-line flags of the windowed EDT passes
+  bm::Buffer qhist, qtargets, qmap;  // quantile histograms, targets, map scratch
   uint32_t surf_max = 0;
 
   // profiler: CUDA events around every library launch while enabled

@@ -63,4 +63,14 @@ cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, c
                              const uint32_t* surf_pts, Dims dm, uint32_t* fillmap, cudaStream_t s,
                              unsigned long long* launches);
 
+// Exact moment sums of f32(raw * scale) over the finite positive raw values.
+cudaError_t launch_moments(const float* map, long long n, float scale, StatsAccum* acc, cudaStream_t s,
+                           unsigned long long* launches);
+// Quantiles (quantile.cu): histogram of the high 16 bits of the positive finite
+// f32 values, and of the low 16 bits for values whose high bits equal one of
+// ntarget (<= 16) targets (hist laid out [target][65536]).
+cudaError_t launch_hist_hi(const float* map, long long n, uint32_t* hist, cudaStream_t s, unsigned long long* launches);
+cudaError_t launch_hist_lo(const float* map, long long n, const uint32_t* targets, int ntarget, uint32_t* hist,
+                           cudaStream_t s, unsigned long long* launches);
+
 }  // namespace bm

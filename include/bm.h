@@ -124,6 +124,16 @@ int bm_tbth_tbsp(bm_ctx* ctx, const uint8_t* bone, const uint8_t* roi, size_t wi
                  size_t depth, double spacing_um, unsigned flags, bm_stats* thickness,
                  bm_stats* spacing, float* thickness_map, float* spacing_map);
 
+/* nonzero_stats of a map of n f32 values (metrics.rs:204-269): over the finite
+ * positive values, v = (raw * (float)scale) as f64; mean / SD / max from exact
+ * sums; with BM_FLAG_QUANTILES also median, P10, P25, P75, P90 (numpy-linear
+ * interpolation of exact order statistics) and IQR.  BM_ERR_EMPTY when no
+ * value is finite and positive (metrics.rs:228-230). */
+int bm_nonzero_stats(bm_ctx* ctx, const float* values, size_t n, double scale, unsigned flags,
+                     bm_stats* out);
+int bm_nonzero_stats_device(bm_ctx* ctx, const float* d_values, size_t n, double scale, unsigned flags,
+                            bm_stats* out, void* stream);
+
 /* Device-pointer variants (inputs and outputs in device memory). */
 int bm_edt_sq_device(bm_ctx* ctx, const uint8_t* d_volume, size_t width, size_t height,
                      size_t depth, int phase, uint32_t* d_out, void* stream);
