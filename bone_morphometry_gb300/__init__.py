@@ -8,10 +8,10 @@ hand-written CUDA kernels behind the C ABI of include/bm.h.
 
 from ._lib import BoneMorphometryError, Context, default_context, library_path, load
 from .api import (BinaryVolume, DistributionStats, FeatureMode, Phase, ThicknessMetrics, analyze_thickness,
-                  euclidean_distance_transform_squared, local_thickness, nonzero_stats)
+                  euclidean_distance_transform_squared, local_thickness, nonzero_stats, volume_metrics)
 
 __all__ = [
     "BinaryVolume", "BoneMorphometryError", "Context", "DistributionStats", "FeatureMode", "Phase",
     "ThicknessMetrics", "analyze_thickness", "default_context", "euclidean_distance_transform_squared",
-    "library_path", "load", "local_thickness", "nonzero_stats",
+    "library_path", "load", "local_thickness", "nonzero_stats", "volume_metrics",
 ]

@@ -63,6 +63,28 @@ class BmStats(ctypes.Structure):
     ]
 
 
+class BmVolumeMetrics(ctypes.Structure):
+    _fields_ = [
+        ("bone_voxels", ctypes.c_uint64),
+        ("roi_voxels", ctypes.c_uint64),
+        ("boundary_bone_voxels", ctypes.c_uint64),
+        ("bone_volume", ctypes.c_double),
+        ("total_volume", ctypes.c_double),
+        ("bone_volume_fraction", ctypes.c_double),
+        ("roi_boundary_bone_fraction", ctypes.c_double),
+    ]
+
+
+class BmSpecimen(ctypes.Structure):
+    _fields_ = [("bone", ctypes.c_void_p), ("roi", ctypes.c_void_p), ("width", ctypes.c_size_t),
+                ("height", ctypes.c_size_t), ("depth", ctypes.c_size_t), ("spacing_um", ctypes.c_double)]
+
+
+class BmResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("thickness", BmStats), ("spacing", BmStats), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("end_s", ctypes.c_double), ("footprint_bytes", ctypes.c_uint64)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/bm.h
 _vp = ctypes.c_void_p
 _sz = ctypes.c_size_t
@@ -91,6 +113,20 @@ SIGNATURES = {
     "bm_edt_sq_device_noalloc": (_i, [_u8p, _sz, _sz, _sz, _i, _vp, _vp]),
     "bm_nonzero_stats": (_i, [_pctx, _vp, _sz, _d, _u, ctypes.POINTER(BmStats)]),
     "bm_nonzero_stats_device": (_i, [_pctx, _vp, _sz, _d, _u, ctypes.POINTER(BmStats), _vp]),
+    "bm_volume_metrics_compute": (_i, [_pctx, _u8p, _u8p, _sz, _sz, _sz, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(BmVolumeMetrics)]),
+    "bm_volume_metrics_device": (_i, [_pctx, _u8p, _u8p, _sz, _sz, _sz, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(BmVolumeMetrics), _vp]),
+    "bm_batch_tbth_tbsp": (_i, [_pctx, ctypes.POINTER(BmSpecimen), _sz, _i, _u, ctypes.POINTER(BmStats),
+                                ctypes.POINTER(BmStats), ctypes.POINTER(ctypes.c_int)]),
+    "bm_ctx_set_workers": (_i, [_pctx, _i]),
+    "bm_server_create": (_i, [_i, _i, _d, ctypes.POINTER(ctypes.c_void_p)]),
+    "bm_server_submit": (_i, [_vp, ctypes.POINTER(BmSpecimen), _u, ctypes.POINTER(ctypes.c_uint64)]),
+    "bm_server_poll": (_i, [_vp, ctypes.c_uint64, _i, ctypes.POINTER(BmResult)]),
+    "bm_server_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                             ctypes.POINTER(ctypes.c_double)]),
+    "bm_server_destroy": (None, [_vp]),
+    "bm_footprint_bytes": (ctypes.c_uint64, [_sz, _sz, _sz]),
 }
 
 _LIB = None

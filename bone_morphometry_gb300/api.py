@@ -25,7 +25,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import (BM_ERR_DIMS, BM_ERR_INVALID, BM_FLAG_BONEJ_ROI, BM_FLAG_QUANTILES, BmStats,
+from ._lib import (BM_ERR_DIMS, BM_ERR_INVALID, BM_FLAG_BONEJ_ROI, BM_FLAG_QUANTILES, BmStats, BmVolumeMetrics,
                    BoneMorphometryError, Context, default_context)
 
 
@@ -229,6 +229,40 @@ def nonzero_stats(values, scale: float, include_quantiles: bool = False, ctx: Co
         v = np.ascontiguousarray(np.asarray(values, dtype=np.float32)).reshape(-1)
         ctx.call("bm_nonzero_stats", _ptr(v), v.size, float(scale), flags, ctypes.byref(out))
     return DistributionStats.from_c(out)
+
+
+@dataclass
+class VolumeMetrics:
+    """metrics.rs:123-132 and 166-202."""
+
+    bone_voxels: int
+    roi_voxels: int
+    boundary_bone_voxels: int
+    bone_volume: float
+    total_volume: float
+    bone_volume_fraction: float
+    roi_boundary_bone_fraction: float
+
+
+def volume_metrics(bone, roi, voxel_spacing, ctx: Context | None = None) -> VolumeMetrics:
+    """BV, TV, BV/TV and the ROI-boundary bone fraction of one specimen."""
+    ctx = ctx or default_context()
+    if isinstance(voxel_spacing, (int, float)):
+        voxel_spacing = (float(voxel_spacing),) * 3
+    sp = (ctypes.c_double * 3)(*[float(v) for v in voxel_spacing])
+    out = BmVolumeMetrics()
+    if _is_cuda_tensor(bone):
+        w, h, d = _tensor_dims(bone)
+        ctx.call("bm_volume_metrics_device", ctypes.c_void_p(bone.data_ptr()), ctypes.c_void_p(roi.data_ptr()),
+                 w, h, d, sp, ctypes.byref(out), _stream_ptr(bone))
+    else:
+        b, r = _as_volume(bone), _as_volume(roi)
+        if not b.same_shape(r):
+            raise BoneMorphometryError(BM_ERR_INVALID, "binary image dimensions do not match ROI dimensions")
+        ctx.call("bm_volume_metrics_compute", _ptr(b.data), _ptr(r.data), b.width, b.height, b.depth, sp,
+                 ctypes.byref(out))
+    return VolumeMetrics(int(out.bone_voxels), int(out.roi_voxels), int(out.boundary_bone_voxels), out.bone_volume,
+                         out.total_volume, out.bone_volume_fraction, out.roi_boundary_bone_fraction)
 
 
 def _flags(feature_mode) -> int:

@@ -491,6 +491,66 @@ __global__ void count_roi_kernel(const uint8_t* __restrict__ bone, const uint8_t
   }
 }
 
+// ROI voxels, ROI-clipped bone voxels, and those of them with a 6-neighbour
+// outside the volume or outside the ROI (metrics.rs:166-202).
+__global__ void volume_counts_kernel(const uint8_t* __restrict__ bone, const uint8_t* __restrict__ roi, Dims dm,
+                                     unsigned long long* __restrict__ out) {
+  unsigned long long c_roi = 0, c_bone = 0, c_edge = 0;
+  const long long n = dm.n();
+  const long long sl = (long long)dm.w * dm.h;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const bool r = roi[i] != 0;
+    c_roi += r;
+    if (r && bone[i] != 0) {
+      ++c_bone;
+      const int z = (int)(i / sl);
+      const long long rem = i - (long long)z * sl;
+      const int y = (int)(rem / dm.w), x = (int)(rem - (long long)y * dm.w);
+      const bool edge = x == 0 || y == 0 || z == 0 || x == dm.w - 1 || y == dm.h - 1 || z == dm.d - 1 ||
+                        roi[i - 1] == 0 || roi[i + 1] == 0 || roi[i - dm.w] == 0 || roi[i + dm.w] == 0 ||
+                        roi[i - sl] == 0 || roi[i + sl] == 0;
+      c_edge += edge;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    c_roi += __shfl_xor_sync(0xffffffffu, c_roi, o);
+    c_bone += __shfl_xor_sync(0xffffffffu, c_bone, o);
+    c_edge += __shfl_xor_sync(0xffffffffu, c_edge, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (c_roi) atomicAdd(&out[0], c_roi);
+    if (c_bone) atomicAdd(&out[1], c_bone);
+    if (c_edge) atomicAdd(&out[2], c_edge);
+  }
+}
+
+int volume_metrics_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, Dims dm, const double* sp,
+                        bm_volume_metrics* out, cudaStream_t s) {
+  for (int i = 0; i < 3; ++i)
+    if (!std::isfinite(sp[i]) || sp[i] <= 0.0)
+      fail(ctx, BM_ERR_SPACING, "voxel spacings must be finite and positive; got [%g, %g, %g]", sp[0], sp[1], sp[2]);
+  unsigned long long* dc = static_cast<unsigned long long*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
+  check(ctx, cudaMemsetAsync(dc, 0, 24, s), "memset");
+  timed(ctx, KF_COUNT_ROI, s, "volume counts", [&] {
+    volume_counts_kernel<<<152 * 8, 256, 0, s>>>(d_bone, d_roi, dm, dc);
+    ++ctx->launches;
+    return cudaGetLastError();
+  });
+  unsigned long long hc[3];
+  check(ctx, cudaMemcpyAsync(hc, dc, 24, cudaMemcpyDeviceToHost, s), "count readback");
+  check(ctx, cudaStreamSynchronize(s), "volume counts");
+  const double voxel_volume = ((1.0 * sp[0]) * sp[1]) * sp[2];  // metrics.rs:123 (product)
+  out->roi_voxels = hc[0];
+  out->bone_voxels = hc[1];
+  out->boundary_bone_voxels = hc[2];
+  out->bone_volume = (double)hc[1] * voxel_volume;
+  out->total_volume = (double)hc[0] * voxel_volume;
+  out->bone_volume_fraction = out->bone_volume / out->total_volume;
+  out->roi_boundary_bone_fraction = (double)hc[2] / (double)hc[1];
+  return BM_OK;
+}
+
 int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, Dims dm, double spacing,
                      unsigned flags, bm_stats* th, bm_stats* sp, float* d_thmap, float* d_spmap, cudaStream_t s) {
   // metrics.rs:70-78
@@ -548,6 +608,17 @@ namespace bm {
 // Message returned by bm_last_error(NULL, ...) on this thread (used by the
 // entry points that take no context).
 void set_thread_error(const char* msg) { g_create_error = msg; }
+
+size_t cached_bytes(const bm_ctx* ctx) {
+  const Buffer* all[] = {&ctx->in_a,     &ctx->in_b,       &ctx->dist,       &ctx->dist2,       &ctx->stack,
+                         &ctx->fillmap,  &ctx->selbits,    &ctx->posbits,    &ctx->ridges,      &ctx->accum,
+                         &ctx->outmap,   &ctx->outmap2,    &ctx->occ,        &ctx->rank,        &ctx->rvals,
+                         &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
+                         &ctx->qhist,    &ctx->qtargets,   &ctx->qmap};
+  size_t t = 0;
+  for (const Buffer* b : all) t += b->bytes;
+  return t;
+}
 }  // namespace bm
 
 extern "C" {
@@ -597,6 +668,11 @@ int bm_ctx_trim(bm_ctx* ctx) {
 
 void bm_ctx_destroy(bm_ctx* ctx) {
   if (!ctx) return;
+  {
+    std::lock_guard<std::mutex> plock(ctx->pool_mu);
+    if (ctx->pool) pool_destroy(ctx->pool);
+    ctx->pool = nullptr;
+  }
   {
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaSetDevice(ctx->device);
@@ -780,6 +856,28 @@ int bm_nonzero_stats(bm_ctx* ctx, const float* values, size_t n, double scale, u
     if (st) return st;
     if (flags & BM_FLAG_QUANTILES) quantiles(ctx, d, (long long)n, ha.count, scale, out, s);
     return BM_OK;
+  });
+}
+
+int bm_volume_metrics_device(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, size_t width, size_t height,
+                             size_t depth, const double spacing_um[3], bm_volume_metrics* out, void* stream) {
+  return guarded(ctx, [&]() -> int {
+    if (!d_bone || !d_roi || !spacing_um || !out) fail(ctx, BM_ERR_INVALID, "null pointer");
+    const Dims dm = check_dims(ctx, width, height, depth);
+    return volume_metrics_impl(ctx, d_bone, d_roi, dm, spacing_um, out, pick_stream(ctx, stream));
+  });
+}
+
+int bm_volume_metrics_compute(bm_ctx* ctx, const uint8_t* bone, const uint8_t* roi, size_t width, size_t height,
+                              size_t depth, const double spacing_um[3], bm_volume_metrics* out) {
+  return guarded(ctx, [&]() -> int {
+    if (!bone || !roi || !spacing_um || !out) fail(ctx, BM_ERR_INVALID, "null pointer");
+    const Dims dm = check_dims(ctx, width, height, depth);
+    const size_t N = (size_t)dm.n();
+    cudaStream_t s = ctx->stream;
+    const uint8_t* d_bone = stage_input(ctx, ctx->in_a, bone, N, s);
+    const uint8_t* d_roi = stage_input(ctx, ctx->in_b, roi, N, s);
+    return volume_metrics_impl(ctx, d_bone, d_roi, dm, spacing_um, out, s);
   });
 }
 

@@ -93,6 +93,9 @@ struct ProfRec {
   cudaEvent_t start, stop;
 };
 
+class Pool;  // worker pool of the batched / served forms (serve.cpp)
+void pool_destroy(Pool* p);
+
 }  // namespace bm
 
 struct bm_ctx {
@@ -133,4 +136,14 @@ struct bm_ctx {
   std::vector<cudaEvent_t> event_pool;
   double prof_ms[bm::KF_COUNT] = {};
   unsigned long long prof_n[bm::KF_COUNT] = {};
+
+  // worker pool used by bm_batch_tbth_tbsp (created on first use)
+  std::mutex pool_mu;
+  bm::Pool* pool = nullptr;
+  int workers = 4;
 };
+
+namespace bm {
+// Device bytes currently cached by a context's buffers.
+size_t cached_bytes(const bm_ctx* ctx);
+}  // namespace bm

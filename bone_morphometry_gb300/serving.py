@@ -1,0 +1,143 @@
+"""Batched and served forms of the Tb.Th / Tb.Sp path (bm_batch_tbth_tbsp and
+bm_server_* in include/bm.h).
+
+``batch_tbth_tbsp`` runs many specimens of uneven sizes through the context's
+native worker pool: each worker owns a CUDA stream and buffers, so several
+specimens are in flight on the GPU at once.  ``Server`` is the request loop:
+submissions are admitted in arrival order while the estimated device footprint
+of the running requests stays within an HBM budget, and each result carries
+submit / start / end timestamps for latency percentiles.  Both use the
+per-specimen arithmetic, so every result equals the specimen's result alone.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import (BM_ERR_BUSY, BM_OK, BmResult, BmSpecimen, BmStats, BoneMorphometryError, Context, default_context,
+                   last_error, load, raise_for)
+from .api import DistributionStats, FeatureMode, _flags, _is_cuda_tensor
+
+
+@dataclass
+class SpecimenInput:
+    bone: object          # (d, h, w) uint8 numpy array or CUDA tensor
+    roi: object
+    spacing_um: float
+
+
+def _specimen_struct(sp: SpecimenInput) -> BmSpecimen:
+    if _is_cuda_tensor(sp.bone):
+        d, h, w = sp.bone.shape
+        return BmSpecimen(sp.bone.data_ptr(), sp.roi.data_ptr(), w, h, d, float(sp.spacing_um))
+    b = np.ascontiguousarray(sp.bone, np.uint8)
+    r = np.ascontiguousarray(sp.roi, np.uint8)
+    if b.shape != r.shape:
+        raise ValueError("bone and roi shapes differ")
+    d, h, w = b.shape
+    return BmSpecimen(b.ctypes.data, r.ctypes.data, w, h, d, float(sp.spacing_um))
+
+
+def batch_tbth_tbsp(specimens, feature_mode=FeatureMode.CLASSIC, ctx: Context | None = None, workers: int | None = None):
+    """Tb.Th / Tb.Sp of every specimen; returns [(thickness, spacing, status)]."""
+    ctx = ctx or default_context()
+    lib = load()
+    if workers is not None:
+        raise_for(lib.bm_ctx_set_workers(ctx.handle, int(workers)), ctx.handle)
+    items = list(specimens)
+    if not items:
+        return []
+    device = _is_cuda_tensor(items[0].bone)
+    keep = []
+    arr = (BmSpecimen * len(items))()
+    for i, sp in enumerate(items):
+        if not device:
+            sp = SpecimenInput(np.ascontiguousarray(sp.bone, np.uint8), np.ascontiguousarray(sp.roi, np.uint8),
+                               sp.spacing_um)
+            keep.append(sp)
+        arr[i] = _specimen_struct(sp)
+    th = (BmStats * len(items))()
+    spc = (BmStats * len(items))()
+    st = (ctypes.c_int * len(items))()
+    lib.bm_batch_tbth_tbsp(ctx.handle, arr, len(items), 1 if device else 0, _flags(feature_mode), th, spc, st)
+    return [(DistributionStats.from_c(th[i]), DistributionStats.from_c(spc[i]), int(st[i])) for i in range(len(items))]
+
+
+def footprint_bytes(shape) -> int:
+    d, h, w = shape
+    return int(load().bm_footprint_bytes(w, h, d))
+
+
+@dataclass
+class Result:
+    ticket: int
+    status: int
+    thickness: DistributionStats
+    spacing: DistributionStats
+    submit_s: float
+    start_s: float
+    end_s: float
+    footprint_bytes: int
+
+    @property
+    def latency_s(self) -> float:
+        return self.end_s - self.submit_s
+
+
+class Server:
+    """Request loop over the native worker pool with HBM-budget admission."""
+
+    def __init__(self, device: int = 0, workers: int = 4, hbm_budget_bytes: float = 120e9):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        st = self._lib.bm_server_create(int(device), int(workers), float(hbm_budget_bytes), ctypes.byref(h))
+        if st != BM_OK:
+            raise BoneMorphometryError(st, last_error(None) or "server creation failed")
+        self.handle = h
+        self._inputs = {}
+
+    def submit(self, bone, roi, spacing_um: float, feature_mode=FeatureMode.CLASSIC) -> int:
+        sp = SpecimenInput(np.ascontiguousarray(bone, np.uint8), np.ascontiguousarray(roi, np.uint8), spacing_um)
+        s = _specimen_struct(sp)
+        t = ctypes.c_uint64()
+        st = self._lib.bm_server_submit(self.handle, ctypes.byref(s), _flags(feature_mode), ctypes.byref(t))
+        if st != BM_OK:
+            raise BoneMorphometryError(st, "request exceeds the HBM budget" if st == BM_ERR_BUSY else "submit failed")
+        self._inputs[t.value] = sp  # keep the host buffers alive until the result is taken
+        return t.value
+
+    def result(self, ticket: int, wait: bool = True):
+        r = BmResult()
+        st = self._lib.bm_server_poll(self.handle, ctypes.c_uint64(ticket), 1 if wait else 0, ctypes.byref(r))
+        if st == BM_ERR_BUSY:
+            return None
+        if st != BM_OK:
+            raise BoneMorphometryError(st, "unknown ticket %d" % ticket)
+        self._inputs.pop(ticket, None)
+        return Result(ticket, r.status, DistributionStats.from_c(r.thickness), DistributionStats.from_c(r.spacing),
+                      r.submit_s, r.start_s, r.end_s, int(r.footprint_bytes))
+
+    def stats(self):
+        q, run, b = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
+        self._lib.bm_server_stats(self.handle, ctypes.byref(q), ctypes.byref(run), ctypes.byref(b))
+        return int(q.value), int(run.value), float(b.value)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.bm_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

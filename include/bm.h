@@ -134,6 +134,28 @@ int bm_nonzero_stats(bm_ctx* ctx, const float* values, size_t n, double scale, u
 int bm_nonzero_stats_device(bm_ctx* ctx, const float* d_values, size_t n, double scale, unsigned flags,
                             bm_stats* out, void* stream);
 
+/* Bone volume block of `analyze` (metrics.rs:123-132, 166-202): with the
+ * ROI-clipped bone (bone != 0 && roi != 0) and voxel volume s0*s1*s2,
+ * bone_volume = bone voxels * voxel volume, total_volume = ROI voxels * voxel
+ * volume, bone_volume_fraction = their ratio, and roi_boundary_bone_fraction =
+ * share of ROI-clipped bone voxels with a 6-neighbour outside the volume or
+ * outside the ROI (NaN without bone). */
+typedef struct bm_volume_metrics {
+  uint64_t bone_voxels;
+  uint64_t roi_voxels;
+  uint64_t boundary_bone_voxels;
+  double bone_volume;
+  double total_volume;
+  double bone_volume_fraction;
+  double roi_boundary_bone_fraction;
+} bm_volume_metrics;
+
+int bm_volume_metrics_compute(bm_ctx* ctx, const uint8_t* bone, const uint8_t* roi, size_t width, size_t height,
+                              size_t depth, const double spacing_um[3], bm_volume_metrics* out);
+int bm_volume_metrics_device(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, size_t width,
+                             size_t height, size_t depth, const double spacing_um[3], bm_volume_metrics* out,
+                             void* stream);
+
 /* Device-pointer variants (inputs and outputs in device memory). */
 int bm_edt_sq_device(bm_ctx* ctx, const uint8_t* d_volume, size_t width, size_t height,
                      size_t depth, int phase, uint32_t* d_out, void* stream);
@@ -161,6 +183,55 @@ int bm_tbth_tbsp_device(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi
  * synchronising it.  Errors: bm_last_error(NULL, ...). */
 int bm_edt_sq_device_noalloc(const uint8_t* d_volume, size_t width, size_t height, size_t depth,
                              int phase, uint32_t* d_out, void* stream);
+
+/* ---- batched and served forms --------------------------------------------
+ * A specimen for the batch and the server: bone and roi are host or device
+ * pointers (see the call), spacing in micrometres.  The buffers must stay
+ * valid until the call (batch) or the ticket (server) completes. */
+typedef struct bm_specimen {
+  const uint8_t* bone;
+  const uint8_t* roi;
+  size_t width, height, depth;
+  double spacing_um;
+} bm_specimen;
+
+/* Tb.Th / Tb.Sp of n specimens of uneven sizes.  The context's worker pool
+ * (bm_ctx_set_workers; by default 4 workers, each with its own stream and
+ * buffers) takes specimens as workers free up, so their kernels overlap on the
+ * GPU.  Per-specimen results and statuses go to thickness[i], spacing[i],
+ * status[i]; the call returns BM_OK when every specimen succeeded, else the
+ * first non-zero status (the others still complete).  device_pointers != 0:
+ * bone/roi are device pointers on the context's device. */
+int bm_batch_tbth_tbsp(bm_ctx* ctx, const bm_specimen* items, size_t n, int device_pointers, unsigned flags,
+                       bm_stats* thickness, bm_stats* spacing, int* status);
+/* Set the number of workers of the context's pool (1..64; recreates the pool). */
+int bm_ctx_set_workers(bm_ctx* ctx, int workers);
+
+/* Request server: submitted specimens (host pointers) are admitted in arrival
+ * order while the estimated device footprint of the requests in flight stays
+ * within hbm_budget_bytes and a worker is free; admitted requests run
+ * concurrently on the workers' streams (continuous batching: a request that
+ * arrives while others run starts as soon as a worker and budget free up).
+ * Results carry per-request timestamps for latency percentiles. */
+typedef struct bm_server bm_server;
+typedef struct bm_result {
+  int status;
+  bm_stats thickness;
+  bm_stats spacing;
+  double submit_s, start_s, end_s; /* seconds on a steady clock */
+  uint64_t footprint_bytes;
+} bm_result;
+int bm_server_create(int device, int workers, double hbm_budget_bytes, bm_server** out);
+/* BM_ERR_BUSY if the request alone exceeds the budget. */
+int bm_server_submit(bm_server* srv, const bm_specimen* item, unsigned flags, uint64_t* ticket);
+/* wait != 0: block until the ticket completes; else BM_ERR_BUSY while pending.
+ * A completed ticket's result is returned once and then forgotten. */
+int bm_server_poll(bm_server* srv, uint64_t ticket, int wait, bm_result* out);
+/* Requests waiting for admission, requests running, bytes in flight. */
+int bm_server_stats(bm_server* srv, uint64_t* queued, uint64_t* running, double* bytes_in_flight);
+void bm_server_destroy(bm_server* srv);
+/* Estimated device bytes one specimen of n voxels occupies while it runs. */
+uint64_t bm_footprint_bytes(size_t width, size_t height, size_t depth);
 
 /* Kernel launches issued by this context since creation (library kernels only). */
 uint64_t bm_ctx_launch_count(const bm_ctx* ctx);

@@ -78,3 +78,35 @@ def test_bonej_mode_rejects_full_roi(gpu_ctx):
     sp = S.config_plain_128()
     with pytest.raises(BoneMorphometryError, match="both inside and outside"):
         analyze_thickness(sp.bone, np.ones_like(sp.roi), sp.spacing_um, FeatureMode.BONEJ, ctx=gpu_ctx)
+
+
+def test_roi_controls_volume_and_boundary_fraction(gpu_ctx):
+    # metrics.rs:328-354 (BV, TV, BV/TV and the ROI boundary bone fraction parts)
+    from bone_morphometry_gb300 import volume_metrics
+
+    bone = np.zeros((5, 5, 5), np.uint8)
+    bone[2, 2, 1] = 1
+    roi = np.zeros((5, 5, 5), np.uint8)
+    roi[1:4, 1:4, 1:4] = 1
+    vm = volume_metrics(bone, roi, 1.0, ctx=gpu_ctx)
+    assert vm.bone_volume == 1.0 and vm.total_volume == 27.0
+    assert abs(vm.bone_volume_fraction - 1.0 / 27.0) < 1e-12
+    assert vm.roi_boundary_bone_fraction == 1.0
+
+
+def test_volume_metrics_random(gpu_ctx):
+    from bone_morphometry_gb300 import volume_metrics
+
+    sp = S.config_plain_128()
+    spacing = (10.0, 11.0, 12.5)
+    vm = volume_metrics(sp.bone, sp.roi, spacing, ctx=gpu_ctx)
+    b = (sp.bone != 0) & (sp.roi != 0)
+    r = sp.roi != 0
+    vv = (1.0 * spacing[0]) * spacing[1] * spacing[2]
+    assert vm.bone_volume == b.sum() * vv and vm.total_volume == r.sum() * vv
+    rp = np.pad(r, 1, constant_values=False)
+    nb = np.zeros_like(b)
+    for ax in range(3):
+        for sh in (-1, 1):
+            nb |= ~np.roll(rp, sh, axis=ax)[1:-1, 1:-1, 1:-1]
+    assert vm.boundary_bone_voxels == int((b & nb).sum())
