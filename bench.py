@@ -73,6 +73,10 @@ def parse_args(argv=None):
     ap.add_argument("--impl", choices=("gpu", "reference"), default="gpu")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="single512")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the 64-specimen batch and the Poisson serving measurements")
+    ap.add_argument("--serve-requests", type=int, default=64)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--cpu-sample-slices", type=int, default=0,
                     help="z-slab depth of the CPU sample (default: sized to ~10 s)")
     return ap.parse_args(argv)
@@ -228,6 +232,139 @@ def run_reference(args, rank, world):
     return 0
 
 
+def percentile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    pos = q * (len(xs) - 1)
+    lo, hi = int(pos), min(int(pos) + 1, len(xs) - 1)
+    return xs[lo] + (pos - lo) * (xs[hi] - xs[lo])
+
+
+def bench_batch(ctx, n_items=64):
+    """64 specimens of uneven sizes: plain per-specimen calls vs the batched
+    form (worker count picked by a short autotune over {2, 4, 6, 8})."""
+    import torch
+
+    from bone_morphometry_gb300 import analyze_thickness
+    from bone_morphometry_gb300 import synthetic as S
+    from bone_morphometry_gb300.serving import SpecimenInput, batch_tbth_tbsp
+
+    specs = S.batch_specs(n_items)
+    items = []
+    for sp in specs:
+        d, h, w = sp.shape
+        t = S.make_specimen_torch(sp.shape, sp.sigma, sp.bvtv, "cylinder", 0.45 * min(w, h), sp.spacing_um, sp.seed,
+                                  to_host=False)
+        items.append(t)
+    torch.cuda.synchronize()
+    vox = sum(int(t.bone.numel()) for t in items)
+    dev = [SpecimenInput(t.bone, t.roi, t.spacing_um) for t in items]
+
+    def plain():
+        out = []
+        for t in items:
+            out.append(analyze_thickness(t.bone, t.roi, t.spacing_um, ctx=ctx))
+        torch.cuda.synchronize()
+        return out
+
+    plain()  # warm buffers
+    t0 = time.perf_counter()
+    ref = plain()
+    t_plain = time.perf_counter() - t0
+    tune = {}
+    for wk in (2, 4, 6, 8):
+        batch_tbth_tbsp(dev, ctx=ctx, workers=wk)
+        t0 = time.perf_counter()
+        batch_tbth_tbsp(dev, ctx=ctx)
+        tune[wk] = time.perf_counter() - t0
+    best = min(tune, key=tune.get)
+    batch_tbth_tbsp(dev, ctx=ctx, workers=best)
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        res = batch_tbth_tbsp(dev, ctx=ctx)
+        times.append(time.perf_counter() - t0)
+    t_batch = min(times)
+    same = all(r[2] == 0 and r[0].mean == a.thickness.mean and r[1].mean == a.spacing.mean
+               and r[0].standard_deviation == a.thickness.standard_deviation for r, a in zip(res, ref))
+    return {"specimens": n_items, "voxels": vox, "plain_gvoxel_s": vox / t_plain / 1e9,
+            "batched_gvoxel_s": vox / t_batch / 1e9, "speedup": t_plain / t_batch, "plain_ms": 1e3 * t_plain,
+            "batched_ms": 1e3 * t_batch, "workers": best,
+            "autotune_ms": {str(k): round(1e3 * v, 2) for k, v in tune.items()},
+            "results_identical_to_plain": bool(same),
+            "data": "torch GPU generator, sizes log-uniform [96,384] per axis"}
+
+
+def bench_serving(n_requests=64, rate=200.0, budget=120e9, workers=4):
+    """Poisson arrivals (rate req/s) of specimens with edges log-uniform in
+    [64, 768]; 24 distinct generated specimens are cycled.  Served form
+    (continuous admission, HBM budget) vs serial plain processing of the same
+    arrival sequence (queueing computed from each specimen's measured plain time)."""
+    import numpy as np
+    import torch
+
+    from bone_morphometry_gb300 import Context, analyze_thickness
+    from bone_morphometry_gb300 import synthetic as S
+    from bone_morphometry_gb300.serving import Server
+
+    specs = S.serving_specs(24)
+    pool = []
+    for sp in specs:
+        d, h, w = sp.shape
+        pool.append(S.make_specimen_torch(sp.shape, sp.sigma, sp.bvtv, "cylinder", 0.45 * min(w, h), sp.spacing_um,
+                                          sp.seed, to_host=True))
+    torch.cuda.empty_cache()
+    rng = np.random.default_rng(1234)
+    gaps = rng.exponential(1.0 / rate, size=n_requests)
+    order = [i % len(pool) for i in range(n_requests)]
+    # serial plain service time of each distinct specimen (host pointers, same path as a request)
+    ctx = Context(0)
+    service = []
+    alone = []
+    for sp in pool:
+        analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=ctx)
+        t0 = time.perf_counter()
+        alone.append(analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=ctx))
+        service.append(time.perf_counter() - t0)
+    ctx.close()
+    # serial plain: one request at a time in arrival order
+    t_arr = np.cumsum(gaps)
+    end = 0.0
+    lat_serial = []
+    for i, k in enumerate(order):
+        start = max(t_arr[i], end)
+        end = start + service[k]
+        lat_serial.append(end - t_arr[i])
+    span_serial = end - t_arr[0]
+    # served
+    with Server(workers=workers, hbm_budget_bytes=budget) as srv:
+        tickets = []
+        t_start = time.perf_counter()
+        for i, k in enumerate(order):
+            target = t_start + t_arr[i] - t_arr[0]
+            delay = target - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            tickets.append((k, srv.submit(pool[k].bone, pool[k].roi, pool[k].spacing_um)))
+        results = [(k, srv.result(t)) for k, t in tickets]
+    first = min(r.submit_s for _, r in results)
+    last = max(r.end_s for _, r in results)
+    lat = [r.latency_s for _, r in results]
+    vox = sum(int(pool[k].bone.size) for k in order)
+    same = all(r.status == 0 and r.thickness.mean == alone[k].thickness.mean
+               and r.spacing.standard_deviation == alone[k].spacing.standard_deviation for k, r in results)
+    return {"requests": n_requests, "offered_req_s": rate, "distinct_specimens": len(pool),
+            "mean_voxels_per_request": vox / n_requests, "hbm_budget_gb": budget / 1e9, "workers": workers,
+            "served_gvoxel_s": vox / (last - first) / 1e9,
+            "served_p50_ms": 1e3 * percentile(lat, 0.5), "served_p99_ms": 1e3 * percentile(lat, 0.99),
+            "serial_plain_gvoxel_s": vox / span_serial / 1e9,
+            "serial_plain_p50_ms": 1e3 * percentile(lat_serial, 0.5),
+            "serial_plain_p99_ms": 1e3 * percentile(lat_serial, 0.99),
+            "results_identical_to_alone": bool(same),
+            "data": "torch GPU generator, edges log-uniform [64,768]; host-pointer requests (H2D inside)"}
+
+
 def run_gpu(args, rank, world, local):
     import numpy as np
     import torch
@@ -340,6 +477,11 @@ def run_gpu(args, rank, world, local):
         cpu = {"value": vox / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "z-slab %dx%dx%d of the same specimen, both phases, %.1f s" % (w, h, slices, dt)}
 
+    extras = {}
+    if world == 1 and not args.no_extras:
+        extras["batch64"] = bench_batch(ctx)
+        extras["serving"] = bench_serving(args.serve_requests, args.serve_rate)
+
     d, h, w = sp.bone.shape
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -364,6 +506,7 @@ def run_gpu(args, rank, world, local):
         "result": {"TbTh_mean_um": res.thickness.mean, "TbTh_sd_um": res.thickness.standard_deviation,
                    "TbSp_mean_um": res.spacing.mean, "TbSp_sd_um": res.spacing.standard_deviation},
     }
+    line.update(extras)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

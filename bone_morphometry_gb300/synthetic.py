@@ -128,3 +128,62 @@ def make_batch_item(spec: BatchItemSpec) -> Specimen:
     d, h, w = spec.shape
     return make_specimen(spec.shape, spec.sigma, spec.bvtv, "cylinder", 0.45 * min(w, h), spec.spacing_um,
                          spec.seed)
+
+
+def make_specimen_torch(shape, sigma, bvtv: float, roi_kind: str, roi_radius: float, spacing_um: float,
+                        seed: int, device: str = "cuda", to_host: bool = True) -> Specimen:
+    """The same generator on the GPU (torch): N(0,1) noise, separable Gaussian
+    filter truncated at 4 sigma with reflected borders, threshold at the
+    (1 - BV/TV) quantile (estimated from a 1/8 subsample above 64 M voxels).
+    Used for the large benchmark workloads, where scipy on the host would take
+    minutes; the voxel pattern differs from make_specimen's for the same seed."""
+    import torch
+    import torch.nn.functional as F
+
+    d, h, w = shape
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    f = torch.randn((1, 1, d, h, w), generator=g, device=device, dtype=torch.float32)
+    sig = sigma if isinstance(sigma, (tuple, list)) else (sigma, sigma, sigma)
+    for axis, s in ((4, sig[0]), (3, sig[1]), (2, sig[2])):  # x, y, z
+        r = int(4.0 * s + 0.5)
+        t = torch.arange(-r, r + 1, device=device, dtype=torch.float32)
+        k = torch.exp(-0.5 * (t / s) ** 2)
+        k = k / k.sum()
+        shape_k = [1, 1, 1, 1, 1]
+        shape_k[axis] = 2 * r + 1
+        pad = [0, 0, 0, 0, 0, 0]
+        pad[2 * (4 - axis)] = r
+        pad[2 * (4 - axis) + 1] = r
+        f = F.conv3d(F.pad(f, pad, mode="reflect"), k.view(shape_k))
+    f = f.view(d, h, w)
+    flat = f.reshape(-1)
+    sample = flat if flat.numel() <= (1 << 26) else flat[:: 8]
+    k = max(1, int(round((1.0 - bvtv) * (sample.numel() - 1))) + 1)
+    thr = torch.kthvalue(sample, k).values
+    bone = torch.where(f > thr, 255, 0).to(torch.uint8)
+    del f, flat, sample
+    if roi_kind == "cylinder":
+        yy = torch.arange(h, device=device, dtype=torch.float64).view(h, 1)
+        xx = torch.arange(w, device=device, dtype=torch.float64).view(1, w)
+        disk = ((xx - (w - 1) / 2.0) ** 2 + (yy - (h - 1) / 2.0) ** 2) <= roi_radius * roi_radius
+        roi = disk.view(1, h, w).expand(d, h, w).to(torch.uint8).contiguous()
+    elif roi_kind == "sphere":
+        zz = torch.arange(d, device=device, dtype=torch.float64).view(d, 1, 1)
+        yy = torch.arange(h, device=device, dtype=torch.float64).view(1, h, 1)
+        xx = torch.arange(w, device=device, dtype=torch.float64).view(1, 1, w)
+        roi = (((xx - (w - 1) / 2.0) ** 2 + (yy - (h - 1) / 2.0) ** 2 + (zz - (d - 1) / 2.0) ** 2)
+               <= roi_radius * roi_radius).to(torch.uint8)
+    else:
+        roi = torch.ones((d, h, w), device=device, dtype=torch.uint8)
+    meta = dict(shape=tuple(shape), sigma=sigma, bvtv=bvtv, roi=roi_kind, roi_radius=roi_radius,
+                spacing_um=spacing_um, seed=seed, generator="torch")
+    if to_host:
+        return Specimen(bone.cpu().numpy(), roi.cpu().numpy(), spacing_um, meta)
+    return Specimen(bone, roi, spacing_um, meta)
+
+
+def serving_specs(n: int = 24, edge_lo: int = 64, edge_hi: int = 768, seed: int = 1005):
+    """Request sizes for the serving workload: per-axis edges log-uniform in
+    [edge_lo, edge_hi], the batch distributions for sigma / BV/TV / spacing."""
+    return batch_specs(n, edge_lo, edge_hi, seed)
