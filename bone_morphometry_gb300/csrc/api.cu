@@ -174,12 +174,13 @@ void fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsign
   const size_t rwords = (size_t)rmax + 2;
   uint32_t* rank = static_cast<uint32_t*>(ensure(ctx, ctx->rank, rwords * 4, "r2 ranks"));
   uint32_t* rvals = static_cast<uint32_t*>(ensure(ctx, ctx->rvals, rwords * 4, "r2 values"));
+  uint4* rgeo = static_cast<uint4*>(ensure(ctx, ctx->rgeo, rwords * sizeof(uint4), "r2 geometry"));
   FillInfo* info = static_cast<FillInfo*>(ensure(ctx, ctx->fillinfo, sizeof(FillInfo), "fill info"));
   uint32_t* scratch = static_cast<uint32_t*>(ensure(ctx, ctx->scanscratch, scan_scratch_words((long long)rwords) * 4,
                                                     "scan scratch"));
   check(ctx, cudaMemsetAsync(info, 0, sizeof(FillInfo), s), "memset");
   timed(ctx, KF_FILL_RANK, s, "rank kernel",
-        [&] { return launch_rank(occ, rank, rmax, rvals, info, scratch, s, &ctx->launches); });
+        [&] { return launch_rank(occ, rank, rmax, rvals, rgeo, info, scratch, s, &ctx->launches); });
   FillInfo hi;
   check(ctx, cudaMemcpyAsync(&hi, info, sizeof hi, cudaMemcpyDeviceToHost, s), "fill info readback");
   check(ctx, cudaStreamSynchronize(s), "rank kernel");
@@ -213,41 +214,44 @@ void fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsign
   }
   ensure_surf(ctx, rmax);
   timed(ctx, KF_FILL, s, "tile fill kernel", [&] {
-    return launch_tile_fill(entries, offsets, rvals, info, selbits, static_cast<const uint32_t*>(ctx->surf_off.ptr),
-                            static_cast<const uint32_t*>(ctx->surf_pts.ptr), dm, F, s, &ctx->launches);
+    return launch_tile_fill(entries, offsets, rvals, rgeo, info, selbits, static_cast<const uint32_t*>(ctx->surf_pts.ptr),
+                            static_cast<const uint32_t*>(ctx->surf_zoff.ptr), dm, F, s, &ctx->launches);
   });
 }
 
-// Lattice points of every sphere |d|^2 = r2 for r2 <= rmax, cached per context.
+// Lattice points of every sphere |d|^2 = r2 for r2 <= rmax (sorted by dz, with
+// per-dz offsets), cached per context.
 void ensure_surf(bm_ctx* ctx, uint32_t rmax) {
   if (ctx->surf_off.ptr && ctx->surf_max >= rmax) return;
   uint32_t target = rmax < 1024 ? 1024 : rmax;
-  if (ctx->surf_off.ptr && target < ctx->surf_max * 2u) target = ctx->surf_max * 2u;
   if (target > kSurfMaxR2) target = kSurfMaxR2 > rmax ? kSurfMaxR2 : rmax;
   cudaStream_t s = ctx->stream;
   const long long n = (long long)target + 2;
   Buffer cnt;
   uint32_t* c = static_cast<uint32_t*>(ensure(ctx, cnt, (size_t)n * 4, "sphere table"));
-  uint32_t* off = nullptr;
   try {
     release(ctx->surf_off);
     release(ctx->surf_pts);
+    release(ctx->surf_zoff);
     ctx->surf_max = 0;
-    off = static_cast<uint32_t*>(ensure(ctx, ctx->surf_off, (size_t)n * 4, "sphere table"));
+    uint32_t* off = static_cast<uint32_t*>(ensure(ctx, ctx->surf_off, (size_t)n * 4, "sphere table"));
+    uint32_t* zoff = static_cast<uint32_t*>(
+        ensure(ctx, ctx->surf_zoff, (size_t)surf_zoff_entries(target) * 4, "sphere table"));
     uint32_t* scratch = static_cast<uint32_t*>(ensure(ctx, ctx->scanscratch, scan_scratch_words(n) * 4, "scan"));
     check(ctx, cudaMemsetAsync(c, 0, (size_t)n * 4, s), "memset");
-    check(ctx, launch_surf(true, 0, target, c, nullptr, nullptr, s, &ctx->launches), "sphere table");
+    check(ctx, launch_surf(true, 0, target, c, nullptr, nullptr, nullptr, s, &ctx->launches), "sphere table");
     check(ctx, launch_scan(c, off, n, scratch, s, &ctx->launches), "sphere table");
     uint32_t total = 0;
     check(ctx, cudaMemcpyAsync(&total, off + target + 1, 4, cudaMemcpyDeviceToHost, s), "sphere table");
     check(ctx, cudaStreamSynchronize(s), "sphere table");
     uint32_t* pts = static_cast<uint32_t*>(ensure(ctx, ctx->surf_pts, ((size_t)total + 1) * 4, "sphere table"));
-    check(ctx, launch_surf(false, 0, target, nullptr, off, pts, s, &ctx->launches), "sphere table");
+    check(ctx, launch_surf(false, 0, target, nullptr, off, pts, zoff, s, &ctx->launches), "sphere table");
     check(ctx, cudaStreamSynchronize(s), "sphere table");
   } catch (...) {
     release(cnt);
     release(ctx->surf_off);
     release(ctx->surf_pts);
+    release(ctx->surf_zoff);
     throw;
   }
   release(cnt);
@@ -614,7 +618,7 @@ size_t cached_bytes(const bm_ctx* ctx) {
                          &ctx->fillmap,  &ctx->selbits,    &ctx->posbits,    &ctx->ridges,      &ctx->accum,
                          &ctx->outmap,   &ctx->outmap2,    &ctx->occ,        &ctx->rank,        &ctx->rvals,
                          &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
-                         &ctx->qhist,    &ctx->qtargets,   &ctx->qmap};
+                         &ctx->qhist,    &ctx->qtargets,   &ctx->qmap,       &ctx->rgeo};
   size_t t = 0;
   for (const Buffer* b : all) t += b->bytes;
   return t;
@@ -660,7 +664,7 @@ int bm_ctx_trim(bm_ctx* ctx) {
                      &ctx->fillmap, &ctx->selbits,  &ctx->posbits,   &ctx->ridges,     &ctx->accum,
                      &ctx->outmap, &ctx->outmap2,  &ctx->occ,       &ctx->rank,       &ctx->rvals,
                      &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
-                     &ctx->qhist, &ctx->qtargets, &ctx->qmap};
+                     &ctx->qhist, &ctx->qtargets, &ctx->qmap, &ctx->rgeo};
     for (Buffer* b : all) release(*b);
     return BM_OK;
   });
@@ -682,7 +686,7 @@ void bm_ctx_destroy(bm_ctx* ctx) {
                      &ctx->counters, &ctx->accum,     &ctx->outmap,     &ctx->outmap2,  &ctx->host_pinned,
                      &ctx->occ,      &ctx->rank,      &ctx->rvals,      &ctx->fillinfo, &ctx->bincounts,
                      &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
-                     &ctx->qhist,    &ctx->qtargets,  &ctx->qmap};
+                     &ctx->qhist,    &ctx->qtargets,  &ctx->qmap,     &ctx->rgeo};
     for (Buffer* b : all) release(*b);
     for (const ProfRec& r : ctx->prof) {
       cudaEventDestroy(r.start);
@@ -691,6 +695,7 @@ void bm_ctx_destroy(bm_ctx* ctx) {
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     release(ctx->surf_off);
     release(ctx->surf_pts);
+    release(ctx->surf_zoff);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
   }
   delete ctx;

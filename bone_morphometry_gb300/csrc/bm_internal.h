@@ -122,10 +122,11 @@ struct bm_ctx {
   bm::Buffer outmap2;
   bm::Buffer host_pinned;      // pinned staging for small readbacks
   bm::Buffer occ, rank, rvals; // per-r^2 flags, ranks, rank -> r^2
+  bm::Buffer rgeo;             // rank -> {r^2, ceil sqrt, floor sqrt, sphere-table z base}
   bm::Buffer fillinfo;         // bm::FillInfo
   bm::Buffer bincounts, binoffsets, binentries, scanscratch;
   // cached sphere lattice-point table for r2 in [0, surf_max]
-  bm::Buffer surf_off, surf_pts;
+  bm::Buffer surf_off, surf_pts, surf_zoff;
   bm::Buffer redo;             // per-line flags of the windowed EDT passes
   bm::Buffer qhist, qtargets, qmap;  // quantile histograms, targets, map scratch
   uint32_t surf_max = 0;

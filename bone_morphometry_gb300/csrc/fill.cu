@@ -41,6 +41,18 @@ __device__ __forceinline__ uint32_t csqrt_u32(uint32_t v) {
   return f * f == v ? f : f + 1;
 }
 
+// Start of the per-dz offsets of r2 in the zoff table: entries dz = -r .. r+1
+// (r = isqrt(r2)) for every smaller r2 come first, 2*isqrt(q) + 2 per q.
+__host__ __device__ __forceinline__ unsigned long long surf_zbase(uint32_t r2) {
+  // sum_{q < r2} isqrt(q) = sum_{k < K} k (2k + 1) + K (r2 - K^2), K = isqrt(r2)
+  unsigned long long K = (unsigned long long)sqrt((double)r2);
+  while (K * K > r2) --K;
+  while ((K + 1) * (K + 1) <= r2) ++K;
+  const unsigned long long sk = (K == 0) ? 0 : (2 * (K - 1) * K * (2 * K - 1) / 6 + K * (K - 1) / 2);
+  const unsigned long long f = sk + K * ((unsigned long long)r2 - K * K);
+  return 2 * f + 2ull * r2;
+}
+
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr long long kScanTile = kScanThreads * kScanItems;
@@ -95,14 +107,17 @@ __global__ void scan_add_kernel(uint32_t* __restrict__ out, long long n, const u
 // rank_desc (so rank_desc[rmax+1] = nR, never rewritten) -> rank_desc[r2] =
 // descending rank of every r2 present, rvals[rank] = r2, info->nR.
 __global__ void rank_finalize_kernel(const uint32_t* __restrict__ occ, uint32_t* __restrict__ rank_desc, uint32_t rmax,
-                                     uint32_t* __restrict__ rvals, FillInfo* __restrict__ info) {
+                                     uint32_t* __restrict__ rvals, uint4* __restrict__ rgeo,
+                                     FillInfo* __restrict__ info) {
   const uint32_t nR = rank_desc[rmax + 1];
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r <= (long long)rmax;
        r += (long long)gridDim.x * blockDim.x) {
     if (occ[r]) {
       const uint32_t rk = nR - 1u - rank_desc[r];
+      const uint32_t R = (uint32_t)r;
       rank_desc[r] = rk;
-      rvals[rk] = (uint32_t)r;
+      rvals[rk] = R;
+      rgeo[rk] = make_uint4(R, csqrt_u32(R), isqrt_u32(R), (uint32_t)surf_zbase(R));
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) info->nR = nR;
@@ -190,8 +205,27 @@ __device__ __forceinline__ uint32_t sel_word(const uint32_t* __restrict__ selbit
   return selbits[((long long)z * dm.h + y) * nw + c];
 }
 
-constexpr int kBinChunk = 1024;   // bins whose offsets / r^2 are staged in shared memory at a time
+constexpr int kBinChunk = 512;    // bins whose offsets / geometry are staged in shared memory at a time
 constexpr int kEntWin = 2048;     // ball entries staged in shared memory at a time
+constexpr int kRotLevels = 6;     // range-OR table levels: spans 1, 2, 4, 8, 16, 32 rows
+constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
+
+// rot[lv][z][y] = OR of the open-voxel masks of rows y .. y + 2^lv - 1 of
+// plane z (rows past the tile edge count as empty).  Built with shuffles, one
+// plane per warp step.
+__device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uint32_t* __restrict__ rot, int warp,
+                                          int lane, int nwarps) {
+  for (int zz = warp; zz < kFillTZ; zz += nwarps) {
+    uint32_t v = usel[zz * kFillTY + lane];
+    rot[zz * 32 + lane] = v;
+#pragma unroll
+    for (int lv = 1; lv < kRotLevels; ++lv) {
+      const uint32_t u = __shfl_down_sync(0xffffffffu, v, 1 << (lv - 1));
+      v |= (lane + (1 << (lv - 1)) < 32) ? u : 0u;
+      rot[(lv * kFillTZ + zz) * 32 + lane] = v;
+    }
+  }
+}
 
 // Half-word index of voxel (row, x) in the u16 value array: pairs of x share a
 // 32-bit word; the word is XOR-swizzled by the row so that threads touching the
@@ -221,29 +255,25 @@ __device__ __forceinline__ int vidx(int row, int x) {
 // paint chord & usel.
 __global__ void __launch_bounds__(kFillThreads, 4)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
-                 const uint32_t* __restrict__ rvals, const FillInfo* __restrict__ info,
-                 const uint32_t* __restrict__ selbits, const uint32_t* __restrict__ surf_off,
-                 const uint32_t* __restrict__ surf_pts, Dims dm, Geom g, uint32_t* __restrict__ fillmap) {
+                 const uint32_t* __restrict__ rvals, const uint4* __restrict__ rgeo, const FillInfo* __restrict__ info,
+                 const uint32_t* __restrict__ selbits, const uint32_t* __restrict__ surf_pts,
+                 const uint32_t* __restrict__ zoff, Dims dm, Geom g, uint32_t* __restrict__ fillmap) {
   extern __shared__ uint32_t smem[];
   uint16_t* val = reinterpret_cast<uint16_t*>(smem);       // kRows * 32 half-words
   uint32_t* usel = smem + kRows * 16;                        // kRows
   uint32_t* usit = usel + kRows;                             // kRows
   uint32_t* pln = usit + kRows;                              // kFillTZ
   uint32_t* boff = pln + kFillTZ;                            // kBinChunk + 1
-  uint32_t* brv = boff + kBinChunk + 1;                      // kBinChunk
-  uint32_t* nzb = brv + kBinChunk;                           // kBinChunk
+  uint4* bgeo = reinterpret_cast<uint4*>(boff + kBinChunk + 4);  // kBinChunk: {r2, rad, isqrt, zbase}
+  uint32_t* nzb = reinterpret_cast<uint32_t*>(bgeo + kBinChunk);  // kBinChunk
   uint32_t* ent = nzb + kBinChunk;                           // kEntWin
+  uint32_t* rot = ent + kEntWin;                             // kRotLevels * kFillTZ * 32
   __shared__ uint32_t s_nnz, s_wlo, s_whi;
-  // ldiv[ny*33 + k] = (k / ny) | (k % ny) << 8 for row counts ny = 1..32 and k = 0..32
-  __shared__ uint16_t ldiv[33 * 33];
-  for (int i = threadIdx.x; i < 33 * 33; i += blockDim.x) {
-    const int ny = i / 33, k = i % 33;
-    ldiv[i] = ny ? (uint16_t)((k / ny) | ((k % ny) << 8)) : (uint16_t)0;
-  }
   const uint32_t nR = info->nR;
   const int nw = dm.nw();
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
+  const int hl = lane & 15, half = lane >> 4;
   for (long long tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x) {
     const int tx = (int)(tile % g.ntx);
     const int ty = (int)((tile / g.ntx) % g.nty);
@@ -286,11 +316,13 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       usit[r] = dil & ~own;
       if (own) atomicOr(&pln[zz], 1u << yy);
     }
+    __syncthreads();
+    build_rot(usel, rot, warp, lane, kFillWarps);
     for (uint32_t b0 = 0; b0 < nR; b0 += kBinChunk) {
       const uint32_t nb = min((uint32_t)kBinChunk, nR - b0);
       __syncthreads();
       for (uint32_t i = tid; i <= nb; i += kFillThreads) boff[i] = off[b0 + i];
-      for (uint32_t i = tid; i < nb; i += kFillThreads) brv[i] = rvals[b0 + i];
+      for (uint32_t i = tid; i < nb; i += kFillThreads) bgeo[i] = rgeo[b0 + i];
       if (tid == 0) s_nnz = 0u;
       __syncthreads();
       // compact the non-empty bins, preserving order (warp ballots + one atomic per warp)
@@ -315,10 +347,12 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       const uint32_t nnz = s_nnz;
       for (uint32_t k = 0; k < nnz; ++k) {
         const uint32_t bl = nzb[k];
-        const uint32_t R = brv[bl];
+        const uint4 gq = bgeo[bl];
+        const uint32_t R = gq.x;
         const uint16_t tag = (uint16_t)(b0 + bl + 1u);
-        const int rad = (int)csqrt_u32(R);
-        const uint32_t p0 = surf_off[R], np = surf_off[R + 1] - p0;
+        const int rad = (int)gq.y;
+        const int rs = (int)gq.z;                          // sphere points have |dz| <= isqrt(r2)
+        const unsigned long long zb = gq.w;
         const uint32_t e = boff[bl + 1];
         for (uint32_t ss = boff[bl]; ss < e;) {
           if (ss < s_wlo || ss >= s_whi) {  // reload the entry window at ss (uniform decision)
@@ -338,48 +372,79 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
           }
           const uint32_t se = min(e, s_whi);
           const uint32_t* eb = ent + (ss - s_wlo);
-          // one warp per ball
-          for (uint32_t bi = warp; bi < se - ss; bi += kFillWarps) {
-            const uint32_t c = eb[bi];
+          // two balls per warp: lanes 0..15 work on ball 2w, lanes 16..31 on ball 2w+1
+          for (uint32_t bp = 2 * warp; bp < se - ss; bp += 2 * kFillWarps) {
+            const uint32_t bi = bp + half;
+            const bool have = bi < se - ss;
+            const uint32_t c = have ? eb[bi] : 0u;
             const int cx = (int)(c & 0x3ffu) - 512, cy = (int)((c >> 10) & 0x3ffu) - 512, cz = (int)(c >> 20) - 512;
-            // sites: lanes over the lattice points of the sphere
-            for (uint32_t p = lane; p < np; p += 32) {
-              const uint32_t pk = surf_pts[p0 + p];
-              const int sx = cx + ((int)(pk << 22) >> 22);
-              const int sy = cy + ((int)(pk << 12) >> 22);
-              const int sz = cz + ((int)(pk << 2) >> 22);
-              if ((unsigned)sx < (unsigned)vx && (unsigned)sy < (unsigned)vy && (unsigned)sz < (unsigned)vz) {
-                const int row = sz * kFillTY + sy;
-                const uint32_t bit = 1u << sx;
-                if (usit[row] & bit) {
-                  atomicAnd(&usit[row], ~bit);
-                  val[vidx(row, sx)] = tag;
+            // sites: the sphere's lattice points on the planes of this tile
+            if (have) {
+              const int dzlo = max(-rs, -cz), dzhi = min(rs, vz - 1 - cz);
+              if (dzlo <= dzhi) {
+                const uint32_t q1 = zoff[zb + (unsigned long long)(dzhi + rs + 1)];
+                for (uint32_t p = zoff[zb + (unsigned long long)(dzlo + rs)] + hl; p < q1; p += 16) {
+                  const uint32_t pk = surf_pts[p];
+                  const int sx = cx + ((int)(pk << 22) >> 22);
+                  const int sy = cy + ((int)(pk << 12) >> 22);
+                  const int sz = cz + ((int)(pk << 2) >> 22);
+                  if ((unsigned)sx < (unsigned)vx && (unsigned)sy < (unsigned)vy) {
+                    const int row = sz * kFillTY + sy;
+                    const uint32_t bit = 1u << sx;
+                    if (usit[row] & bit) {
+                      atomicAnd(&usit[row], ~bit);
+                      val[vidx(row, sx)] = tag;
+                    }
+                  }
                 }
               }
             }
-            // selected voxels: lanes walk the rows of the ball's box inside the tile
+            // selected voxels.  Lane hl of each half takes plane zlo+hl of its
+            // ball: the plane needs work only if some open row in the disk's
+            // y-range has an unpainted voxel inside the disk's widest chord
+            // (range-OR table; a stale table is a superset, so it never skips
+            // work).  Then, plane by plane, all 32 lanes take one row each.
             const int zlo = max(cz - rad, 0), zhi = min(cz + rad, vz - 1);
-            const int ylo = max(cy - rad, 0), yhi = min(cy + rad, vy - 1);
-            if (zlo > zhi || ylo > yhi) continue;
-            const int ny = yhi - ylo + 1;
-            const int nrows = (zhi - zlo + 1) * ny;
-            const uint32_t dv = ldiv[ny * 33 + lane], st = ldiv[ny * 33 + 32];
-            int zz = zlo + (int)(dv & 0xffu), yy = ylo + (int)(dv >> 8);
-            const int stepz = (int)(st & 0xffu), stepy = (int)(st >> 8);
-            for (int r = lane; r < nrows; r += 32) {
-              if ((pln[zz] >> yy) & 1u) {
-                const int dz = zz - cz, dy = yy - cy;
-                const uint32_t dyz = (uint32_t)(dz * dz + dy * dy);
-                if (dyz <= R) {
-                  const int row = zz * kFillTY + yy;
-                  const uint32_t m = usel[row];
-                  const int hx = (int)isqrt_u32(R - dyz);
-                  const int xa = max(cx - hx, 0), xb = min(cx + hx, vx - 1);
-                  if (m && xa <= xb) {
+            uint32_t prem = 0u;
+            int pya = 0, pyb = -1;
+            bool pass = false;
+            if (have && zlo + hl <= zhi) {
+              const int zz = zlo + hl, dz = zz - cz;
+              if ((uint32_t)(dz * dz) <= R) {
+                prem = R - (uint32_t)(dz * dz);
+                const int hy = (int)isqrt_u32(prem);
+                pya = max(cy - hy, 0);
+                pyb = min(cy + hy, vy - 1);
+                const int xa = max(cx - hy, 0), xb = min(cx + hy, vx - 1);
+                if (pya <= pyb && xa <= xb) {
+                  const int span = pyb - pya + 1;
+                  const int lv = 31 - __clz(span);  // 2^lv <= span
+                  const uint32_t* tl = rot + (lv * kFillTZ + zz) * 32;
+                  const uint32_t orr = tl[pya] | tl[pyb - (1 << lv) + 1];
+                  pass = (orr & range_mask(xa, xb)) != 0u;
+                }
+              }
+            }
+            unsigned active = __ballot_sync(0xffffffffu, pass);
+            while (active) {
+              const int k = __ffs(active) - 1;
+              active &= active - 1u;
+              const uint32_t rem = __shfl_sync(0xffffffffu, prem, k);
+              const int ya = __shfl_sync(0xffffffffu, pya, k), yb = __shfl_sync(0xffffffffu, pyb, k);
+              const int zz = __shfl_sync(0xffffffffu, zlo, k) + (k & 15);
+              const int bx = __shfl_sync(0xffffffffu, cx, k), by = __shfl_sync(0xffffffffu, cy, k);
+              if (lane >= ya && lane <= yb) {  // lane = row y of plane zz
+                const int row = zz * kFillTY + lane;
+                const uint32_t m = usel[row];
+                if (m) {
+                  const int dy = lane - by;
+                  const int hx = (int)isqrt_u32(rem - (uint32_t)(dy * dy));
+                  const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
+                  if (xa <= xb) {
                     uint32_t bits = m & range_mask(xa, xb);
                     if (bits) {
                       const uint32_t old = atomicAnd(&usel[row], ~bits);
-                      if ((old & ~bits) == 0u) atomicAnd(&pln[zz], ~(1u << yy));
+                      if ((old & ~bits) == 0u) atomicAnd(&pln[zz], ~(1u << lane));
                       while (bits) {
                         const int xx = __ffs(bits) - 1;
                         val[vidx(row, xx)] = tag;
@@ -389,17 +454,15 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
                   }
                 }
               }
-              yy += stepy;
-              zz += stepz;
-              if (yy > yhi) {
-                yy -= ny;
-                ++zz;
-              }
             }
           }
           ss = se;
         }
         __syncthreads();
+        if (k % kRotEvery == kRotEvery - 1) {
+          build_rot(usel, rot, warp, lane, kFillWarps);
+          __syncthreads();
+        }
       }
     }
     __syncthreads();
@@ -415,43 +478,45 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
   }
 }
 
-// Lattice points of the sphere |d|^2 = r2: one warp per r2, lanes over dz.
-// COUNT: surf_cnt[r2] = number of points; else write them packed
-// (10-bit two's-complement dx | dy << 10 | dz << 20) from surf_off[r2] on.
+// Lattice points of the sphere |d|^2 = r2: one warp per r2.  COUNT:
+// surf_cnt[r2] = number of points.  Else write them packed (10-bit two's
+// complement dx | dy << 10 | dz << 20) from surf_off[r2] on, sorted by dz, and
+// zoff[surf_zbase(r2) + dz + r] = index of the first point with that dz
+// (entry 2r+1 = end), so a tile can visit only the planes it holds.
 template <bool COUNT>
 __global__ void __launch_bounds__(256)
 surf_kernel(uint32_t lo, uint32_t hi, uint32_t* __restrict__ surf_cnt, const uint32_t* __restrict__ surf_off,
-            uint32_t* __restrict__ surf_pts) {
+            uint32_t* __restrict__ surf_pts, uint32_t* __restrict__ zoff) {
   const int lane = threadIdx.x & 31;
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long rr = (long long)lo + wid; rr <= (long long)hi; rr += nwarps) {
     const uint32_t R = (uint32_t)rr;
     const int r = (int)isqrt_u32(R);
-    uint32_t mine = 0;
-    for (int dz = -r + lane; dz <= r; dz += 32) {
-      const uint32_t rz = R - (uint32_t)(dz * dz);
-      const int ry = (int)isqrt_u32(rz);
-      for (int dy = -ry; dy <= ry; ++dy) {
-        const uint32_t rx2 = rz - (uint32_t)(dy * dy);
-        const uint32_t k = isqrt_u32(rx2);
-        if (k * k == rx2) mine += k ? 2u : 1u;
+    uint32_t total = 0;
+    uint32_t pos0 = COUNT ? 0u : surf_off[R];
+    const unsigned long long zb = COUNT ? 0ull : surf_zbase(R);
+    for (int c0 = -r; c0 <= r; c0 += 32) {
+      const int dz = c0 + lane;
+      uint32_t mine = 0;
+      if (dz <= r) {
+        const uint32_t rz = R - (uint32_t)(dz * dz);
+        const int ry = (int)isqrt_u32(rz);
+        for (int dy = -ry; dy <= ry; ++dy) {
+          const uint32_t rx2 = rz - (uint32_t)(dy * dy);
+          const uint32_t k = isqrt_u32(rx2);
+          if (k * k == rx2) mine += k ? 2u : 1u;
+        }
       }
-    }
-    if (COUNT) {
-      uint32_t cnt = mine;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-      if (lane == 0) surf_cnt[R] = cnt;
-    } else {
       uint32_t incl = mine;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += u;
       }
-      uint32_t pos = surf_off[R] + incl - mine;
-      for (int dz = -r + lane; dz <= r; dz += 32) {
+      if (!COUNT && dz <= r) {
+        uint32_t pos = pos0 + incl - mine;
+        zoff[zb + (unsigned long long)(dz + r)] = pos;
         const uint32_t rz = R - (uint32_t)(dz * dz);
         const int ry = (int)isqrt_u32(rz);
         for (int dy = -ry; dy <= ry; ++dy) {
@@ -463,6 +528,14 @@ surf_kernel(uint32_t lo, uint32_t hi, uint32_t* __restrict__ surf_cnt, const uin
           if (k) surf_pts[pos++] = ((uint32_t)(-(int)k) & 0x3ffu) | yz;
         }
       }
+      const uint32_t chunk = __shfl_sync(0xffffffffu, incl, 31);
+      pos0 += chunk;
+      total += chunk;
+    }
+    if (COUNT) {
+      if (lane == 0) surf_cnt[R] = total;
+    } else if (lane == 0) {
+      zoff[zb + (unsigned long long)(2 * r + 1)] = pos0;
     }
   }
 }
@@ -512,11 +585,12 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, long long n, uint32_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_rank(const uint32_t* occ, uint32_t* rank_desc, uint32_t rmax, uint32_t* rvals, FillInfo* info,
-                        uint32_t* scan_scratch, cudaStream_t s, unsigned long long* launches) {
+cudaError_t launch_rank(const uint32_t* occ, uint32_t* rank_desc, uint32_t rmax, uint32_t* rvals, uint4* rgeo,
+                        FillInfo* info, uint32_t* scan_scratch, cudaStream_t s, unsigned long long* launches) {
   cudaError_t e = launch_scan(occ, rank_desc, (long long)rmax + 2, scan_scratch, s, launches);
   if (e != cudaSuccess) return e;
-  rank_finalize_kernel<<<blocks_for((long long)rmax + 1, 256, 1024), 256, 0, s>>>(occ, rank_desc, rmax, rvals, info);
+  rank_finalize_kernel<<<blocks_for((long long)rmax + 1, 256, 1024), 256, 0, s>>>(occ, rank_desc, rmax, rvals, rgeo,
+                                                                                  info);
   ++*launches;
   return cudaGetLastError();
 }
@@ -534,30 +608,33 @@ cudaError_t launch_bin(bool count, const uint2* ridges, const Counters* ctr, uns
   return cudaGetLastError();
 }
 
+unsigned long long surf_zoff_entries(uint32_t rmax) { return surf_zbase(rmax + 1); }
+
 cudaError_t launch_surf(bool count, uint32_t lo, uint32_t hi, uint32_t* surf_cnt, const uint32_t* surf_off,
-                        uint32_t* surf_pts, cudaStream_t s, unsigned long long* launches) {
+                        uint32_t* surf_pts, uint32_t* zoff, cudaStream_t s, unsigned long long* launches) {
   if (hi < lo) return cudaSuccess;
   const unsigned blocks = blocks_for((long long)hi - lo + 1, 8, 152 * 16);
   if (count)
-    surf_kernel<true><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts);
+    surf_kernel<true><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts, zoff);
   else
-    surf_kernel<false><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts);
+    surf_kernel<false><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts, zoff);
   ++*launches;
   return cudaGetLastError();
 }
 
 cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
-                             const FillInfo* info, const uint32_t* selbits, const uint32_t* surf_off,
-                             const uint32_t* surf_pts, Dims dm, uint32_t* fillmap, cudaStream_t s,
+                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, const uint32_t* surf_pts,
+                             const uint32_t* zoff, Dims dm, uint32_t* fillmap, cudaStream_t s,
                              unsigned long long* launches) {
   const Geom g = geom_of(dm);
   const size_t smem =
-      (size_t)(kRows * 16 + 2 * kRows + kFillTZ + (kBinChunk + 1) + 2 * kBinChunk + kEntWin) * sizeof(uint32_t);
+      (size_t)(kRows * 16 + 2 * kRows + kFillTZ + (kBinChunk + 4) + 4 * kBinChunk + kBinChunk + kEntWin +
+               kRotLevels * kFillTZ * 32) * sizeof(uint32_t);
   cudaError_t e = cudaFuncSetAttribute(tile_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const long long grid = g.ntiles < (1LL << 31) - 1 ? g.ntiles : (1LL << 31) - 1;
-  tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, info, selbits, surf_off,
-                                                               surf_pts, dm, g, fillmap);
+  tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, rgeo, info, selbits, surf_pts,
+                                                               zoff, dm, g, fillmap);
   ++*launches;
   return cudaGetLastError();
 }
