@@ -94,6 +94,10 @@ def make_specimen(workload: str, rank: int):
 
     maker = getattr(S, WORKLOADS[workload]["maker"])
     base = maker.__defaults__[0]
+    if workload == "single1024":
+        # scipy on the host would take minutes for 1 G voxels: same recipe on the GPU
+        return S.make_specimen_torch((1024, 1024, 1024), (4.0, 4.0, 8.0), 0.30, "sphere", 500.0, 8.0,
+                                     base + 7919 * rank)
     return maker(seed=base + 7919 * rank)
 
 

@@ -163,6 +163,9 @@ void ensure_lut(bm_ctx* ctx, uint32_t rmax) {
   ctx->lut.ptr = p;
   ctx->lut.bytes = bytes;
   ctx->lut_max = target;
+  float* dia = static_cast<float*>(ensure(ctx, ctx->lutf, ((size_t)target + 1) * sizeof(float), "diameter table"));
+  check(ctx, launch_dia_table(static_cast<const uint4*>(p), target + 1, dia, ctx->stream, &ctx->launches),
+        "diameter table");
 }
 
 void ensure_surf(bm_ctx* ctx, uint32_t rmax);
@@ -315,7 +318,10 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));
   check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
   timed(ctx, KF_CLEAN_FINAL, s, "cleanup",
-        [&] { return launch_cleanup(F, selbits, dm, lut, scale, d_map, acc, s, &ctx->launches); });
+        [&] {
+          return launch_cleanup(F, selbits, dm, static_cast<const float*>(ctx->lutf.ptr), scale, d_map, acc, s,
+                                &ctx->launches);
+        });
   check(ctx, cudaMemcpyAsync(&res.acc, acc, sizeof(StatsAccum), cudaMemcpyDeviceToHost, s), "stats readback");
   check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
   check(ctx, cudaStreamSynchronize(s), "local thickness");
@@ -696,6 +702,7 @@ void bm_ctx_destroy(bm_ctx* ctx) {
     release(ctx->surf_off);
     release(ctx->surf_pts);
     release(ctx->surf_zoff);
+    release(ctx->lutf);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
   }
   delete ctx;

@@ -109,6 +109,7 @@ struct bm_ctx {
   // cached search-template table: lut[r2] = {t100, t110, t111, 0}
   bm::Buffer lut;
   uint32_t lut_max = 0;  // entries 0..lut_max are valid
+  bm::Buffer lutf;       // f32 diameters 2*sqrt(r2), r2 = 0..lut_max
 
   bm::Buffer in_a, in_b;       // staged host inputs
   bm::Buffer dist, dist2;      // u32 EDT ping/pong

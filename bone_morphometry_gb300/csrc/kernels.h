@@ -38,8 +38,10 @@ cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long 
                         uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
 
 // Fused cleanup passes 1 and 2, phase mask, optional f32 map, exact statistics.
-cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const uint4* lut, float scale,
+// dia: f32 diameters 2*sqrt(r2) by r2 (launch_dia_table).
+cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const float* dia, float scale,
                            float* outmap, StatsAccum* acc, cudaStream_t s, unsigned long long* launches);
+cudaError_t launch_dia_table(const uint4* lut, uint32_t n, float* dia, cudaStream_t s, unsigned long long* launches);
 
 // Tile-owned fill (fill.cu).
 long long fill_tile_count(Dims dm);

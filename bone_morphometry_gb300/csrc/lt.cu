@@ -97,9 +97,12 @@ fill_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, 
   }
 }
 
+
+
 // NEIGHBORS_26 of local_thickness.rs:285-312 (Fiji's visitation order), which
-// fixes the order of the f32 sum in pass 2.
-__constant__ signed char kN26[26][3] = {
+// fixes the order of the f32 sum in cleanup pass 2; constant so that the
+// unrolled loop addresses shared memory with immediate offsets.
+__device__ constexpr signed char kN26c[26][3] = {
     {0, 0, -1}, {0, 0, 1},  {0, -1, 0}, {0, 1, 0},   {-1, 0, 0},  {1, 0, 0},  {0, 1, -1},
     {0, 1, 1},  {1, -1, 0}, {1, 1, 0},  {-1, 0, 1},  {1, 0, 1},   {0, -1, -1}, {0, -1, 1},
     {-1, -1, 0}, {-1, 1, 0}, {-1, 0, -1}, {1, 0, -1}, {1, 1, 1},   {1, -1, 1}, {-1, 1, 1},
@@ -123,7 +126,7 @@ constexpr int kCleanThreads = 256;
 
 __global__ void __launch_bounds__(kCleanThreads)
 cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict__ selbits, Dims dm,
-                    const uint4* __restrict__ lut, float scale, float* __restrict__ outmap,
+                    const float* __restrict__ dia, float scale, float* __restrict__ outmap,
                     StatsAccum* __restrict__ acc, int ntx, int nty, int ntz) {
   __shared__ uint32_t T[kCSZ * kCSY * kCSX];         // f32 diameter bits of the r^2 map
   __shared__ unsigned long long nz[kCSZ * kCSY];     // bit x: T != 0 (or out of volume)
@@ -157,13 +160,13 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
       int x = x0 - kCH + lane;
       uint32_t v = (rin && x >= 0 && x < dm.w) ? row[x] : kOob;
       // staged as the f32 diameter bits (2*sqrt(r^2)); 0 stays 0
-      srow[lane] = (v == 0u || v == kOob) ? 0u : lut[v].w;
+      srow[lane] = (v == 0u || v == kOob) ? 0u : __float_as_uint(dia[v]);
       unsigned b = __ballot_sync(0xffffffffu, v != 0u);
       uint32_t v2 = kOob;
       if (lane < kCSX - 32) {
         x = x0 - kCH + 32 + lane;
         v2 = (rin && x < dm.w) ? row[x] : kOob;
-        srow[32 + lane] = (v2 == 0u || v2 == kOob) ? 0u : lut[v2].w;
+        srow[32 + lane] = (v2 == 0u || v2 == kOob) ? 0u : __float_as_uint(dia[v2]);
       }
       const unsigned b2 = __ballot_sync(0xffffffffu, lane < kCSX - 32 && v2 != 0u);
       const unsigned o1 = __ballot_sync(0xffffffffu, v != 0u && v != kOob);
@@ -206,13 +209,22 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
           if ((inr[sz * kCSY + sy] >> sx) & 1ull) {
             val = own;
           } else {
+            // interior flags of the 3x3x3 neighbourhood, bit (dz+1)*9 + (dy+1)*3 + (dx+1)
+            uint32_t cube = 0;
+#pragma unroll
+            for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+              for (int dy = -1; dy <= 1; ++dy)
+                cube |= (uint32_t)((inr[(sz + dz) * kCSY + sy + dy] >> (sx - 1)) & 7ull)
+                        << ((dz + 1) * 9 + (dy + 1) * 3);
+            const uint32_t* tc = T + (sz * kCSY + sy) * kCSX + sx;
             int count = 0;
             float sum = 0.0f;
 #pragma unroll
-            for (int k = 0; k < 26; ++k) {
-              const int nx = sx + kN26[k][0], ny = sy + kN26[k][1], nzz = sz + kN26[k][2];
-              if ((inr[nzz * kCSY + ny] >> nx) & 1ull) {
-                sum = __fadd_rn(sum, __uint_as_float(T[(nzz * kCSY + ny) * kCSX + nx]));
+            for (int k = 0; k < 26; ++k) {  // NEIGHBORS_26 order (compile-time offsets)
+              const int ci = (kN26c[k][2] + 1) * 9 + (kN26c[k][1] + 1) * 3 + (kN26c[k][0] + 1);
+              if (cube & (1u << ci)) {
+                sum = __fadd_rn(sum, __uint_as_float(tc[(kN26c[k][2] * kCSY + kN26c[k][1]) * kCSX + kN26c[k][0]]));
                 ++count;
               }
             }
@@ -353,6 +365,11 @@ ridge_tile_kernel(const uint32_t* __restrict__ dist, Dims dm, const uint4* __res
   }
 }
 
+__global__ void dia_extract_kernel(const uint4* __restrict__ lut, uint32_t n, float* __restrict__ dia) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    dia[i] = __uint_as_float(lut[i].w);
+}
+
 inline unsigned grid_for(long long work, int per_block, int cap) {
   long long b = (work + per_block - 1) / per_block;
   if (b < 1) b = 1;
@@ -366,6 +383,12 @@ cudaError_t launch_lut(uint4* lut, uint32_t lo, uint32_t hi, cudaStream_t s, uns
   if (hi < lo) return cudaSuccess;
   const long long count = (long long)hi - lo + 1;
   lut_kernel<<<grid_for(count, 8, 152 * 16), 256, 0, s>>>(lut, lo, hi);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dia_table(const uint4* lut, uint32_t n, float* dia, cudaStream_t s, unsigned long long* launches) {
+  dia_extract_kernel<<<grid_for(n, 256, 1024), 256, 0, s>>>(lut, n, dia);
   ++*launches;
   return cudaGetLastError();
 }
@@ -387,12 +410,12 @@ cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long 
   return cudaGetLastError();
 }
 
-cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const uint4* lut, float scale,
+cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const float* dia, float scale,
                            float* outmap, StatsAccum* acc, cudaStream_t s, unsigned long long* launches) {
   const int ntx = (dm.w + kCTX - 1) / kCTX, nty = (dm.h + kCTY - 1) / kCTY, ntz = (dm.d + kCTZ - 1) / kCTZ;
   const long long tiles = (long long)ntx * nty * ntz;
   const unsigned grid = (unsigned)(tiles < 152 * 8 ? tiles : 152 * 8);
-  cleanup_tile_kernel<<<grid, kCleanThreads, 0, s>>>(fillmap, selbits, dm, lut, scale, outmap, acc, ntx, nty, ntz);
+  cleanup_tile_kernel<<<grid, kCleanThreads, 0, s>>>(fillmap, selbits, dm, dia, scale, outmap, acc, ntx, nty, ntz);
   ++*launches;
   return cudaGetLastError();
 }
