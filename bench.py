@@ -374,6 +374,7 @@ def run_gpu(args, rank, world, local):
     import torch
 
     from bone_morphometry_gb300 import Context, analyze_thickness
+    from bone_morphometry_gb300.replicas import max_over_ranks
 
     torch.cuda.set_device(local)
     dist = None
@@ -416,10 +417,7 @@ def run_gpu(args, rank, world, local):
     ctx.profile(False)
     ms = ev0.elapsed_time(ev1) / args.steps
     assert res.thickness.mean == ref_res.thickness.mean and res.spacing.mean == ref_res.spacing.mean
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms)
     value = world * n_vox / (ms * 1e-3) / 1e9
 
     # -- end-to-end leg through the host-pointer entry point (pinned host inputs) --------------
@@ -436,10 +434,7 @@ def run_gpu(args, rank, world, local):
         res_e = analyze_thickness(hbn, hrn, sp.spacing_um, ctx=ctx)
     e2e_s = (time.perf_counter() - t0) / args.steps
     assert res_e.thickness.mean == ref_res.thickness.mean
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s)
     e2e_value = world * n_vox / e2e_s / 1e9
 
     if rank != 0:
