@@ -51,7 +51,7 @@ ALGO_BYTES_PER_VOXEL = {
     "fill_rank": 0.0,                  # per-r^2 tables only
     "fill_bin": 0.0,                   # per-ridge work (ridge records in, bin entries out)
     "templates": 0.0,
-    "cleanup_interior": 4.0 + 0.125,   # map in, bits out
+    "fill_sites": 0.0,                 # per-ridge work (sphere points of each ridge)
     "cleanup_final": 4.0 + 0.25,       # map in, two bitmasks in
     "count_roi": 2.0,
 }

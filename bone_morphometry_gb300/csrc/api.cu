@@ -75,7 +75,7 @@ void release(Buffer& b) {
 
 const char* const kFamilyName[KF_COUNT] = {"count_roi", "edt_x",     "edt_y",           "edt_z",
                                             "templates", "ridge",     "fill",            "fill_rank",
-                                            "fill_bin",  "cleanup_interior", "cleanup_final",
+                                            "fill_bin",  "fill_sites",      "cleanup_final",
                                             "quantile"};
 
 cudaEvent_t pooled_event(bm_ctx* ctx) {
@@ -217,13 +217,15 @@ void fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsign
   }
   ensure_surf(ctx, rmax);
   timed(ctx, KF_FILL, s, "tile fill kernel", [&] {
-    return launch_tile_fill(entries, offsets, rvals, rgeo, info, selbits, static_cast<const uint32_t*>(ctx->surf_pts.ptr),
-                            static_cast<const uint32_t*>(ctx->surf_zoff.ptr), dm, F, s, &ctx->launches);
+    return launch_tile_fill(entries, offsets, rvals, rgeo, info, selbits, dm, F, s, &ctx->launches);
+  });
+  timed(ctx, KF_FILL_SITES, s, "site kernel", [&] {
+    return launch_sites(ridges, ctr, max_ridges, selbits, static_cast<const uint32_t*>(ctx->surf_off.ptr),
+                        static_cast<const uint32_t*>(ctx->surf_pts.ptr), dm, F, s, &ctx->launches);
   });
 }
 
-// Lattice points of every sphere |d|^2 = r2 for r2 <= rmax (sorted by dz, with
-// per-dz offsets), cached per context.
+// Lattice points of every sphere |d|^2 = r2 for r2 <= rmax, cached per context.
 void ensure_surf(bm_ctx* ctx, uint32_t rmax) {
   if (ctx->surf_off.ptr && ctx->surf_max >= rmax) return;
   uint32_t target = rmax < 1024 ? 1024 : rmax;
@@ -235,26 +237,22 @@ void ensure_surf(bm_ctx* ctx, uint32_t rmax) {
   try {
     release(ctx->surf_off);
     release(ctx->surf_pts);
-    release(ctx->surf_zoff);
     ctx->surf_max = 0;
     uint32_t* off = static_cast<uint32_t*>(ensure(ctx, ctx->surf_off, (size_t)n * 4, "sphere table"));
-    uint32_t* zoff = static_cast<uint32_t*>(
-        ensure(ctx, ctx->surf_zoff, (size_t)surf_zoff_entries(target) * 4, "sphere table"));
     uint32_t* scratch = static_cast<uint32_t*>(ensure(ctx, ctx->scanscratch, scan_scratch_words(n) * 4, "scan"));
     check(ctx, cudaMemsetAsync(c, 0, (size_t)n * 4, s), "memset");
-    check(ctx, launch_surf(true, 0, target, c, nullptr, nullptr, nullptr, s, &ctx->launches), "sphere table");
+    check(ctx, launch_surf(true, 0, target, c, nullptr, nullptr, s, &ctx->launches), "sphere table");
     check(ctx, launch_scan(c, off, n, scratch, s, &ctx->launches), "sphere table");
     uint32_t total = 0;
     check(ctx, cudaMemcpyAsync(&total, off + target + 1, 4, cudaMemcpyDeviceToHost, s), "sphere table");
     check(ctx, cudaStreamSynchronize(s), "sphere table");
     uint32_t* pts = static_cast<uint32_t*>(ensure(ctx, ctx->surf_pts, ((size_t)total + 1) * 4, "sphere table"));
-    check(ctx, launch_surf(false, 0, target, nullptr, off, pts, zoff, s, &ctx->launches), "sphere table");
+    check(ctx, launch_surf(false, 0, target, nullptr, off, pts, s, &ctx->launches), "sphere table");
     check(ctx, cudaStreamSynchronize(s), "sphere table");
   } catch (...) {
     release(cnt);
     release(ctx->surf_off);
     release(ctx->surf_pts);
-    release(ctx->surf_zoff);
     throw;
   }
   release(cnt);
@@ -701,7 +699,6 @@ void bm_ctx_destroy(bm_ctx* ctx) {
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     release(ctx->surf_off);
     release(ctx->surf_pts);
-    release(ctx->surf_zoff);
     release(ctx->lutf);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
   }

@@ -82,7 +82,7 @@ enum KernelFamily : int {
   KF_FILL,
   KF_FILL_RANK,
   KF_FILL_BIN,
-  KF_CLEAN_INTERIOR,
+  KF_FILL_SITES,
   KF_CLEAN_FINAL,
   KF_QUANTILE,
   KF_COUNT
@@ -127,7 +127,7 @@ struct bm_ctx {
   bm::Buffer fillinfo;         // bm::FillInfo
   bm::Buffer bincounts, binoffsets, binentries, scanscratch;
   // cached sphere lattice-point table for r2 in [0, surf_max]
-  bm::Buffer surf_off, surf_pts, surf_zoff;
+  bm::Buffer surf_off, surf_pts;
   bm::Buffer redo;             // per-line flags of the windowed EDT passes
   bm::Buffer qhist, qtargets, qmap;  // quantile histograms, targets, map scratch
   uint32_t surf_max = 0;

@@ -20,7 +20,8 @@
 //                          and the ball reaches)
 //   scan(counts)       -> offsets
 //   bin_kernel<SCATTER>-> entries[offset..] = ball centre (linear index)
-//   tile_fill_kernel   -> u32 r^2 map
+//   tile_fill_kernel   -> u32 r^2 map of the selected voxels
+//   site_kernel        -> non-selected voxels on each ridge sphere (atomic max)
 #include "kernels.h"
 
 namespace bm {
@@ -41,16 +42,15 @@ __device__ __forceinline__ uint32_t csqrt_u32(uint32_t v) {
   return f * f == v ? f : f + 1;
 }
 
-// Start of the per-dz offsets of r2 in the zoff table: entries dz = -r .. r+1
-// (r = isqrt(r2)) for every smaller r2 come first, 2*isqrt(q) + 2 per q.
-__host__ __device__ __forceinline__ unsigned long long surf_zbase(uint32_t r2) {
-  // sum_{q < r2} isqrt(q) = sum_{k < K} k (2k + 1) + K (r2 - K^2), K = isqrt(r2)
-  unsigned long long K = (unsigned long long)sqrt((double)r2);
-  while (K * K > r2) --K;
-  while ((K + 1) * (K + 1) <= r2) ++K;
-  const unsigned long long sk = (K == 0) ? 0 : (2 * (K - 1) * K * (2 * K - 1) / 6 + K * (K - 1) / 2);
-  const unsigned long long f = sk + K * ((unsigned long long)r2 - K * K);
-  return 2 * f + 2ull * r2;
+// floor(sqrt(v)) for v < 2^24 from the hardware reciprocal square root: the
+// estimate v * rsqrt(v) is within far less than one of sqrt(v) there, so one
+// integer correction step each way makes the floor exact.
+__device__ __forceinline__ uint32_t isqrt24(uint32_t v) {
+  const float f = (float)v;
+  uint32_t r = (uint32_t)(f * rsqrtf(fmaxf(f, 1.0f)));
+  r -= (r * r > v) ? 1u : 0u;
+  r += ((r + 1) * (r + 1) <= v) ? 1u : 0u;
+  return r;
 }
 
 constexpr int kScanThreads = 1024;
@@ -117,7 +117,7 @@ __global__ void rank_finalize_kernel(const uint32_t* __restrict__ occ, uint32_t*
       const uint32_t R = (uint32_t)r;
       rank_desc[r] = rk;
       rvals[rk] = R;
-      rgeo[rk] = make_uint4(R, csqrt_u32(R), isqrt_u32(R), (uint32_t)surf_zbase(R));
+      rgeo[rk] = make_uint4(R, csqrt_u32(R), isqrt_u32(R), 0u);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) info->nR = nR;
@@ -205,24 +205,23 @@ __device__ __forceinline__ uint32_t sel_word(const uint32_t* __restrict__ selbit
   return selbits[((long long)z * dm.h + y) * nw + c];
 }
 
-constexpr int kBinChunk = 512;    // bins whose offsets / geometry are staged in shared memory at a time
-constexpr int kEntWin = 2048;     // ball entries staged in shared memory at a time
-constexpr int kRotLevels = 6;     // range-OR table levels: spans 1, 2, 4, 8, 16, 32 rows
+constexpr int kBinChunk = 512;    // bins whose offsets are staged in shared memory at a time
+constexpr int kEntWin = 1024;     // ball entries staged in shared memory at a time
+constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself)
 constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
 
-// rot[lv][z][y] = OR of the open-voxel masks of rows y .. y + 2^lv - 1 of
-// plane z (rows past the tile edge count as empty).  Built with shuffles, one
-// plane per warp step.
+// rot[lv - 1][z][y] = OR of the unpainted-voxel masks of rows y .. y + 2^lv - 1
+// of plane z (rows past the tile edge count as empty), lv = 1 .. 5.  Built
+// with shuffles, one plane per warp step.
 __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uint32_t* __restrict__ rot, int warp,
                                           int lane, int nwarps) {
   for (int zz = warp; zz < kFillTZ; zz += nwarps) {
     uint32_t v = usel[zz * kFillTY + lane];
-    rot[zz * 32 + lane] = v;
 #pragma unroll
     for (int lv = 1; lv < kRotLevels; ++lv) {
       const uint32_t u = __shfl_down_sync(0xffffffffu, v, 1 << (lv - 1));
       v |= (lane + (1 << (lv - 1)) < 32) ? u : 0u;
-      rot[(lv * kFillTZ + zz) * 32 + lane] = v;
+      rot[((lv - 1) * kFillTZ + zz) * 32 + lane] = v;
     }
   }
 }
@@ -234,41 +233,43 @@ __device__ __forceinline__ int vidx(int row, int x) {
   return row * 32 + (((((x >> 1) ^ (row & 15)) << 1)) | (x & 1));
 }
 
-// One CTA per tile (32 x 32 x 16 voxels).  Shared memory:
+constexpr size_t kTileFillSmemWords =
+    (size_t)kRows * 16 + kRows + kFillTZ + (kBinChunk + 4) + kBinChunk + kEntWin + (kRotLevels - 1) * kFillTZ * 32;
+
+// One CTA per tile (32 x 32 x 16 voxels) paints the tile's selected voxels.
+// Shared memory:
 //   val  : u16 per voxel, 0 = unpainted, else 1 + rank of the r^2 painted
 //          (rank 0 = largest r^2 present);
 //   usel : per row (z, y), the selected voxels not yet painted;
-//   usit : per row, the sites a ball can still paint.  A ball centred on a
-//          selected voxel p has r^2 = squared distance to p's nearest site, so
-//          it covers a site only when the site lies exactly on its sphere, and
-//          such a site has a selected 26-neighbour (one step towards p): usit
-//          starts as the sites of the selection's 3x3x3 dilation;
 //   pln  : per plane z, the rows whose usel is not empty;
-//   boff / brv / nzb : the tile's bin offsets, bin r^2 and the list of
-//          non-empty bins for the current chunk of bins;
+//   boff / nzb : the tile's bin offsets and the list of non-empty bins for
+//          the current chunk of bins;
 //   ent  : a window of the tile's ball entries, decoded to tile-local
-//          coordinates (10 bits each, biased by 512).
+//          coordinates (10 bits each, biased by 512);
+//   rot  : range-OR table of usel (build_rot).
 // Bins arrive largest r^2 first with a barrier between bins, so the first ball
 // to reach a voxel carries its final value and later balls skip decided
-// voxels.  Inside a bin the work is flattened over the CTA: (ball, sphere
-// point) pairs paint sites, (ball, plane) pairs walk the plane's open rows and
-// paint chord & usel.
+// voxels.  Inside a bin each warp takes two balls (one per half-warp): lane hl
+// of a half tests plane zlo + hl of its ball -- the plane needs work only if
+// some open row in the disk's y-range has an unpainted voxel inside the disk's
+// widest chord (a stale range-OR table is a superset, so it never skips work)
+// -- and then, plane by plane, all 32 lanes take one row each and paint the
+// chord's unpainted voxels.  Non-selected voxels are left 0 here; the site
+// pass adds the ones a sphere reaches.
 __global__ void __launch_bounds__(kFillThreads, 4)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
                  const uint32_t* __restrict__ rvals, const uint4* __restrict__ rgeo, const FillInfo* __restrict__ info,
-                 const uint32_t* __restrict__ selbits, const uint32_t* __restrict__ surf_pts,
-                 const uint32_t* __restrict__ zoff, Dims dm, Geom g, uint32_t* __restrict__ fillmap) {
+                 const uint32_t* __restrict__ selbits, Dims dm, Geom g, uint32_t* __restrict__ fillmap) {
   extern __shared__ uint32_t smem[];
   uint16_t* val = reinterpret_cast<uint16_t*>(smem);       // kRows * 32 half-words
   uint32_t* usel = smem + kRows * 16;                        // kRows
-  uint32_t* usit = usel + kRows;                             // kRows
-  uint32_t* pln = usit + kRows;                              // kFillTZ
+  uint32_t* pln = usel + kRows;                              // kFillTZ
   uint32_t* boff = pln + kFillTZ;                            // kBinChunk + 1
-  uint4* bgeo = reinterpret_cast<uint4*>(boff + kBinChunk + 4);  // kBinChunk: {r2, rad, isqrt, zbase}
-  uint32_t* nzb = reinterpret_cast<uint32_t*>(bgeo + kBinChunk);  // kBinChunk
+  uint32_t* nzb = boff + kBinChunk + 4;                      // kBinChunk
   uint32_t* ent = nzb + kBinChunk;                           // kEntWin
-  uint32_t* rot = ent + kEntWin;                             // kRotLevels * kFillTZ * 32
+  uint32_t* rot = ent + kEntWin;                             // (kRotLevels - 1) * kFillTZ * 32
   __shared__ uint32_t s_nnz, s_wlo, s_whi;
+  __shared__ uint32_t wcnt[kFillWarps];
   const uint32_t nR = info->nR;
   const int nw = dm.nw();
   const int tid = threadIdx.x;
@@ -299,21 +300,9 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
     __syncthreads();
     for (int r = tid; r < kRows; r += kFillThreads) {
       const int zz = r / kFillTY, yy = r % kFillTY;
-      uint32_t own = 0u, dil = 0u;
-      if (zz < vz && yy < vy) {
-        const int z = z0 + zz, y = y0 + yy;
-        uint32_t c = 0u, lft = 0u, rgt = 0u;
-        for (int dz = -1; dz <= 1; ++dz)
-          for (int dy = -1; dy <= 1; ++dy) {
-            c |= sel_word(selbits, dm, nw, z + dz, y + dy, tx);
-            lft |= sel_word(selbits, dm, nw, z + dz, y + dy, tx - 1);
-            rgt |= sel_word(selbits, dm, nw, z + dz, y + dy, tx + 1);
-          }
-        own = sel_word(selbits, dm, nw, z, y, tx) & xmask;
-        dil = (c | (c << 1) | (c >> 1) | (lft >> 31) | (rgt << 31)) & xmask;
-      }
+      uint32_t own = 0u;
+      if (zz < vz && yy < vy) own = selbits[((long long)(z0 + zz) * dm.h + (y0 + yy)) * nw + tx] & xmask;
       usel[r] = own;
-      usit[r] = dil & ~own;
       if (own) atomicOr(&pln[zz], 1u << yy);
     }
     __syncthreads();
@@ -322,7 +311,6 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       const uint32_t nb = min((uint32_t)kBinChunk, nR - b0);
       __syncthreads();
       for (uint32_t i = tid; i <= nb; i += kFillThreads) boff[i] = off[b0 + i];
-      for (uint32_t i = tid; i < nb; i += kFillThreads) bgeo[i] = rgeo[b0 + i];
       if (tid == 0) s_nnz = 0u;
       __syncthreads();
       // compact the non-empty bins, preserving order (warp ballots + one atomic per warp)
@@ -330,7 +318,6 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
         const uint32_t i = base + tid;
         const bool ne = i < nb && boff[i] != boff[i + 1];
         const unsigned m = __ballot_sync(0xffffffffu, ne);
-        __shared__ uint32_t wcnt[kFillWarps];
         if (lane == 0) wcnt[warp] = __popc(m);
         __syncthreads();
         uint32_t before = 0;
@@ -347,12 +334,10 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       const uint32_t nnz = s_nnz;
       for (uint32_t k = 0; k < nnz; ++k) {
         const uint32_t bl = nzb[k];
-        const uint4 gq = bgeo[bl];
+        const uint4 gq = rgeo[b0 + bl];
         const uint32_t R = gq.x;
         const uint16_t tag = (uint16_t)(b0 + bl + 1u);
-        const int rad = (int)gq.y;
-        const int rs = (int)gq.z;                          // sphere points have |dz| <= isqrt(r2)
-        const unsigned long long zb = gq.w;
+        const int rad = (int)gq.z;                         // isqrt(r2): no lattice point of the ball is further
         const uint32_t e = boff[bl + 1];
         for (uint32_t ss = boff[bl]; ss < e;) {
           if (ss < s_wlo || ss >= s_whi) {  // reload the entry window at ss (uniform decision)
@@ -372,73 +357,54 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
           }
           const uint32_t se = min(e, s_whi);
           const uint32_t* eb = ent + (ss - s_wlo);
-          // two balls per warp: lanes 0..15 work on ball 2w, lanes 16..31 on ball 2w+1
+          // two balls per warp: lanes 0..15 test ball 2w, lanes 16..31 ball 2w+1
           for (uint32_t bp = 2 * warp; bp < se - ss; bp += 2 * kFillWarps) {
             const uint32_t bi = bp + half;
             const bool have = bi < se - ss;
             const uint32_t c = have ? eb[bi] : 0u;
             const int cx = (int)(c & 0x3ffu) - 512, cy = (int)((c >> 10) & 0x3ffu) - 512, cz = (int)(c >> 20) - 512;
-            // sites: the sphere's lattice points on the planes of this tile
-            if (have) {
-              const int dzlo = max(-rs, -cz), dzhi = min(rs, vz - 1 - cz);
-              if (dzlo <= dzhi) {
-                const uint32_t q1 = zoff[zb + (unsigned long long)(dzhi + rs + 1)];
-                for (uint32_t p = zoff[zb + (unsigned long long)(dzlo + rs)] + hl; p < q1; p += 16) {
-                  const uint32_t pk = surf_pts[p];
-                  const int sx = cx + ((int)(pk << 22) >> 22);
-                  const int sy = cy + ((int)(pk << 12) >> 22);
-                  const int sz = cz + ((int)(pk << 2) >> 22);
-                  if ((unsigned)sx < (unsigned)vx && (unsigned)sy < (unsigned)vy) {
-                    const int row = sz * kFillTY + sy;
-                    const uint32_t bit = 1u << sx;
-                    if (usit[row] & bit) {
-                      atomicAnd(&usit[row], ~bit);
-                      val[vidx(row, sx)] = tag;
-                    }
-                  }
-                }
-              }
-            }
-            // selected voxels.  Lane hl of each half takes plane zlo+hl of its
-            // ball: the plane needs work only if some open row in the disk's
-            // y-range has an unpainted voxel inside the disk's widest chord
-            // (range-OR table; a stale table is a superset, so it never skips
-            // work).  Then, plane by plane, all 32 lanes take one row each.
             const int zlo = max(cz - rad, 0), zhi = min(cz + rad, vz - 1);
-            uint32_t prem = 0u;
-            int pya = 0, pyb = -1;
             bool pass = false;
             if (have && zlo + hl <= zhi) {
               const int zz = zlo + hl, dz = zz - cz;
-              if ((uint32_t)(dz * dz) <= R) {
-                prem = R - (uint32_t)(dz * dz);
-                const int hy = (int)isqrt_u32(prem);
-                pya = max(cy - hy, 0);
-                pyb = min(cy + hy, vy - 1);
+              const int prem = (int)R - dz * dz;
+              if (prem >= 0) {
+                const int hy = (int)isqrt24((uint32_t)prem);
+                const int pya = max(cy - hy, 0), pyb = min(cy + hy, vy - 1);
                 const int xa = max(cx - hy, 0), xb = min(cx + hy, vx - 1);
                 if (pya <= pyb && xa <= xb) {
                   const int span = pyb - pya + 1;
                   const int lv = 31 - __clz(span);  // 2^lv <= span
-                  const uint32_t* tl = rot + (lv * kFillTZ + zz) * 32;
-                  const uint32_t orr = tl[pya] | tl[pyb - (1 << lv) + 1];
+                  uint32_t orr;
+                  if (lv == 0) {
+                    orr = usel[zz * kFillTY + pya];
+                  } else {
+                    const uint32_t* tl = rot + ((lv - 1) * kFillTZ + zz) * 32;
+                    orr = tl[pya] | tl[pyb - (1 << lv) + 1];
+                  }
                   pass = (orr & range_mask(xa, xb)) != 0u;
                 }
               }
             }
             unsigned active = __ballot_sync(0xffffffffu, pass);
+            if (!active) continue;
+            // both balls' centres in every lane (the two halves swap theirs)
+            const uint32_t co = __shfl_xor_sync(0xffffffffu, c, 16);
+            const uint32_t c0 = half ? co : c, c1 = half ? c : co;
             while (active) {
               const int k = __ffs(active) - 1;
               active &= active - 1u;
-              const uint32_t rem = __shfl_sync(0xffffffffu, prem, k);
-              const int ya = __shfl_sync(0xffffffffu, pya, k), yb = __shfl_sync(0xffffffffu, pyb, k);
-              const int zz = __shfl_sync(0xffffffffu, zlo, k) + (k & 15);
-              const int bx = __shfl_sync(0xffffffffu, cx, k), by = __shfl_sync(0xffffffffu, cy, k);
-              if (lane >= ya && lane <= yb) {  // lane = row y of plane zz
+              const uint32_t cb = (k & 16) ? c1 : c0;
+              const int bx = (int)(cb & 0x3ffu) - 512, by = (int)((cb >> 10) & 0x3ffu) - 512;
+              const int bz = (int)(cb >> 20) - 512;
+              const int zz = max(bz - rad, 0) + (k & 15);
+              const int dz = zz - bz, dy = lane - by;
+              const int t = (int)R - dz * dz - dy * dy;  // lane = row y of plane zz
+              if (t >= 0) {
                 const int row = zz * kFillTY + lane;
                 const uint32_t m = usel[row];
                 if (m) {
-                  const int dy = lane - by;
-                  const int hx = (int)isqrt_u32(rem - (uint32_t)(dy * dy));
+                  const int hx = (int)isqrt24((uint32_t)t);
                   const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
                   if (xa <= xb) {
                     uint32_t bits = m & range_mask(xa, xb);
@@ -478,15 +444,48 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
   }
 }
 
+// The non-selected voxels a ridge ball reaches.  A ball centred on p has r^2 =
+// d^2(p), the squared distance from p to its nearest non-selected voxel, so the
+// non-selected voxels inside it are exactly the non-selected lattice points of
+// its sphere |v - p|^2 = r^2.  Half a warp per ridge, lanes over the sphere's
+// points; the map keeps the max over balls.  Runs after the tile fill, which
+// leaves every non-selected voxel at 0.
+__global__ void __launch_bounds__(256)
+site_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, const uint32_t* __restrict__ selbits,
+            const uint32_t* __restrict__ surf_off, const uint32_t* __restrict__ surf_pts, Dims dm,
+            uint32_t* __restrict__ fillmap) {
+  const unsigned long long nr = ctr->ridges;
+  const int hl = threadIdx.x & 15;
+  const int nw = dm.nw();
+  const long long hw0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+  const long long nhw = ((long long)gridDim.x * blockDim.x) >> 4;
+  for (long long i = hw0; i < (long long)nr; i += nhw) {
+    const uint2 rec = ridges[i];
+    const uint32_t R = rec.y;
+    int x, y, z;
+    decode(rec.x, dm, x, y, z);
+    const uint32_t p1 = surf_off[R + 1];
+    for (uint32_t p = surf_off[R] + hl; p < p1; p += 16) {
+      const uint32_t pk = surf_pts[p];
+      const int sx = x + ((int)(pk << 22) >> 22);
+      const int sy = y + ((int)(pk << 12) >> 22);
+      const int sz = z + ((int)(pk << 2) >> 22);
+      if ((unsigned)sx >= (unsigned)dm.w || (unsigned)sy >= (unsigned)dm.h || (unsigned)sz >= (unsigned)dm.d) continue;
+      const uint32_t wbits = selbits[((long long)sz * dm.h + sy) * nw + (sx >> 5)];
+      if ((wbits >> (sx & 31)) & 1u) continue;  // selected: painted by the tile fill
+      uint32_t* dst = fillmap + ((long long)sz * dm.h + sy) * dm.w + sx;
+      if (*dst < R) atomicMax(dst, R);
+    }
+  }
+}
+
 // Lattice points of the sphere |d|^2 = r2: one warp per r2.  COUNT:
 // surf_cnt[r2] = number of points.  Else write them packed (10-bit two's
-// complement dx | dy << 10 | dz << 20) from surf_off[r2] on, sorted by dz, and
-// zoff[surf_zbase(r2) + dz + r] = index of the first point with that dz
-// (entry 2r+1 = end), so a tile can visit only the planes it holds.
+// complement dx | dy << 10 | dz << 20) from surf_off[r2] on.
 template <bool COUNT>
 __global__ void __launch_bounds__(256)
 surf_kernel(uint32_t lo, uint32_t hi, uint32_t* __restrict__ surf_cnt, const uint32_t* __restrict__ surf_off,
-            uint32_t* __restrict__ surf_pts, uint32_t* __restrict__ zoff) {
+            uint32_t* __restrict__ surf_pts) {
   const int lane = threadIdx.x & 31;
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -495,7 +494,6 @@ surf_kernel(uint32_t lo, uint32_t hi, uint32_t* __restrict__ surf_cnt, const uin
     const int r = (int)isqrt_u32(R);
     uint32_t total = 0;
     uint32_t pos0 = COUNT ? 0u : surf_off[R];
-    const unsigned long long zb = COUNT ? 0ull : surf_zbase(R);
     for (int c0 = -r; c0 <= r; c0 += 32) {
       const int dz = c0 + lane;
       uint32_t mine = 0;
@@ -516,7 +514,6 @@ surf_kernel(uint32_t lo, uint32_t hi, uint32_t* __restrict__ surf_cnt, const uin
       }
       if (!COUNT && dz <= r) {
         uint32_t pos = pos0 + incl - mine;
-        zoff[zb + (unsigned long long)(dz + r)] = pos;
         const uint32_t rz = R - (uint32_t)(dz * dz);
         const int ry = (int)isqrt_u32(rz);
         for (int dy = -ry; dy <= ry; ++dy) {
@@ -532,11 +529,7 @@ surf_kernel(uint32_t lo, uint32_t hi, uint32_t* __restrict__ surf_cnt, const uin
       pos0 += chunk;
       total += chunk;
     }
-    if (COUNT) {
-      if (lane == 0) surf_cnt[R] = total;
-    } else if (lane == 0) {
-      zoff[zb + (unsigned long long)(2 * r + 1)] = pos0;
-    }
+    if (COUNT && lane == 0) surf_cnt[R] = total;
   }
 }
 
@@ -608,33 +601,37 @@ cudaError_t launch_bin(bool count, const uint2* ridges, const Counters* ctr, uns
   return cudaGetLastError();
 }
 
-unsigned long long surf_zoff_entries(uint32_t rmax) { return surf_zbase(rmax + 1); }
-
 cudaError_t launch_surf(bool count, uint32_t lo, uint32_t hi, uint32_t* surf_cnt, const uint32_t* surf_off,
-                        uint32_t* surf_pts, uint32_t* zoff, cudaStream_t s, unsigned long long* launches) {
+                        uint32_t* surf_pts, cudaStream_t s, unsigned long long* launches) {
   if (hi < lo) return cudaSuccess;
   const unsigned blocks = blocks_for((long long)hi - lo + 1, 8, 152 * 16);
   if (count)
-    surf_kernel<true><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts, zoff);
+    surf_kernel<true><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts);
   else
-    surf_kernel<false><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts, zoff);
+    surf_kernel<false><<<blocks, 256, 0, s>>>(lo, hi, surf_cnt, surf_off, surf_pts);
   ++*launches;
   return cudaGetLastError();
 }
 
 cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
-                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, const uint32_t* surf_pts,
-                             const uint32_t* zoff, Dims dm, uint32_t* fillmap, cudaStream_t s,
-                             unsigned long long* launches) {
+                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm,
+                             uint32_t* fillmap, cudaStream_t s, unsigned long long* launches) {
   const Geom g = geom_of(dm);
-  const size_t smem =
-      (size_t)(kRows * 16 + 2 * kRows + kFillTZ + (kBinChunk + 4) + 4 * kBinChunk + kBinChunk + kEntWin +
-               kRotLevels * kFillTZ * 32) * sizeof(uint32_t);
+  const size_t smem = kTileFillSmemWords * sizeof(uint32_t);
   cudaError_t e = cudaFuncSetAttribute(tile_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const long long grid = g.ntiles < (1LL << 31) - 1 ? g.ntiles : (1LL << 31) - 1;
-  tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, rgeo, info, selbits, surf_pts,
-                                                               zoff, dm, g, fillmap);
+  tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, rgeo, info, selbits, dm, g,
+                                                               fillmap);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sites(const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
+                         const uint32_t* selbits, const uint32_t* surf_off, const uint32_t* surf_pts, Dims dm,
+                         uint32_t* fillmap, cudaStream_t s, unsigned long long* launches) {
+  const unsigned blocks = blocks_for((long long)max_ridges, 16, 152 * 16);
+  site_kernel<<<blocks, 256, 0, s>>>(ridges, ctr, selbits, surf_off, surf_pts, dm, fillmap);
   ++*launches;
   return cudaGetLastError();
 }

@@ -50,23 +50,25 @@ size_t scan_scratch_words(long long n);
 cudaError_t launch_scan(const uint32_t* in, uint32_t* out, long long n, uint32_t* scratch, cudaStream_t s,
                         unsigned long long* launches);
 // occ[0..rmax+1] (occ[rmax+1] == 0) -> rank_desc / rvals / info->nR.
-// rgeo[rank] = {r2, ceil sqrt, floor sqrt, sphere-table z base} for every rank.
+// rgeo[rank] = {r2, ceil sqrt, floor sqrt, 0} for every rank.
 cudaError_t launch_rank(const uint32_t* occ, uint32_t* rank_desc, uint32_t rmax, uint32_t* rvals, uint4* rgeo,
                         FillInfo* info, uint32_t* scan_scratch, cudaStream_t s, unsigned long long* launches);
 cudaError_t launch_bin(bool count, const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
                        const uint32_t* rank_desc, FillInfo* info, Dims dm, uint32_t* counts,
                        const uint32_t* offsets, uint32_t* entries, cudaStream_t s, unsigned long long* launches);
 // Sphere lattice-point table: count (surf_cnt[r2]) or fill (surf_pts from surf_off[r2]) for r2 in [lo, hi].
-// zoff: per-(r2, dz) start offsets (surf_zoff_entries(rmax) entries).
-unsigned long long surf_zoff_entries(uint32_t rmax);
 cudaError_t launch_surf(bool count, uint32_t lo, uint32_t hi, uint32_t* surf_cnt, const uint32_t* surf_off,
-                        uint32_t* surf_pts, uint32_t* zoff, cudaStream_t s, unsigned long long* launches);
-// selbits: the phase's row-padded selection bitmask (edt_x output); surf_off /
-// surf_pts: the lattice-point table covering every ridge r2.
+                        uint32_t* surf_pts, cudaStream_t s, unsigned long long* launches);
+// Selected voxels of every tile from the binned balls; non-selected voxels get 0.
+// selbits: the phase's row-padded selection bitmask (edt_x output).
 cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
-                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, const uint32_t* surf_pts,
-                             const uint32_t* zoff, Dims dm, uint32_t* fillmap, cudaStream_t s,
-                             unsigned long long* launches);
+                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm,
+                             uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
+// Non-selected voxels on each ridge's sphere: atomic max of r2 (after the tile
+// fill).  surf_off / surf_pts: the lattice-point table covering every ridge r2.
+cudaError_t launch_sites(const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
+                         const uint32_t* selbits, const uint32_t* surf_off, const uint32_t* surf_pts, Dims dm,
+                         uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
 
 // Exact moment sums of f32(raw * scale) over the finite positive raw values.
 cudaError_t launch_moments(const float* map, long long n, float scale, StatsAccum* acc, cudaStream_t s,
