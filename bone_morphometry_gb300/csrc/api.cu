@@ -202,7 +202,7 @@ void fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsign
         [&] { return launch_scan(counts, offsets, nbins + 1, scratch, s, &ctx->launches); });
   check(ctx, cudaMemcpyAsync(&hi, info, sizeof hi, cudaMemcpyDeviceToHost, s), "fill info readback");
   check(ctx, cudaStreamSynchronize(s), "bin kernels");
-  if (hi.total_entries >= 0xFFFFFFFFull || rmax > kSurfMaxR2) {
+  if (hi.total_entries >= 0xFFFFFFFFull || rmax > kSurfMaxR2 || hi.nR >= 0xFFFFu) {
     check(ctx, cudaMemsetAsync(F, 0, (size_t)dm.n() * 4, s), "memset");
     timed(ctx, KF_FILL, s, "fill kernel",
           [&] { return launch_fill(ridges, ctr, max_ridges, dm, F, s, &ctx->launches); });

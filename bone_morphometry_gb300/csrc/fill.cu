@@ -205,10 +205,12 @@ __device__ __forceinline__ uint32_t sel_word(const uint32_t* __restrict__ selbit
   return selbits[((long long)z * dm.h + y) * nw + c];
 }
 
-constexpr int kBinChunk = 512;    // bins whose offsets are staged in shared memory at a time
+constexpr int kBinChunk = 256;    // bins whose offsets are staged in shared memory at a time
 constexpr int kEntWin = 1024;     // ball entries staged in shared memory at a time
 constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself)
 constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
+constexpr int kItems = 1024;      // (ball, plane) paint items per round
+constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
 
 // rot[lv - 1][z][y] = OR of the unpainted-voxel masks of rows y .. y + 2^lv - 1
 // of plane z (rows past the tile edge count as empty), lv = 1 .. 5.  Built
@@ -234,28 +236,31 @@ __device__ __forceinline__ int vidx(int row, int x) {
 }
 
 constexpr size_t kTileFillSmemWords =
-    (size_t)kRows * 16 + kRows + kFillTZ + (kBinChunk + 4) + kBinChunk + kEntWin + (kRotLevels - 1) * kFillTZ * 32;
+    (size_t)kRows * 16 + kRows + (kBinChunk + 4) + kBinChunk + kEntWin + (kRotLevels - 1) * kFillTZ * 32 + kItems;
 
 // One CTA per tile (32 x 32 x 16 voxels) paints the tile's selected voxels.
 // Shared memory:
 //   val  : u16 per voxel, 0 = unpainted, else 1 + rank of the r^2 painted
 //          (rank 0 = largest r^2 present);
 //   usel : per row (z, y), the selected voxels not yet painted;
-//   pln  : per plane z, the rows whose usel is not empty;
 //   boff / nzb : the tile's bin offsets and the list of non-empty bins for
 //          the current chunk of bins;
 //   ent  : a window of the tile's ball entries, decoded to tile-local
 //          coordinates (10 bits each, biased by 512);
-//   rot  : range-OR table of usel (build_rot).
+//   rot  : range-OR table of usel (build_rot);
+//   item : the (ball, plane) pairs of the current round that need painting.
 // Bins arrive largest r^2 first with a barrier between bins, so the first ball
 // to reach a voxel carries its final value and later balls skip decided
-// voxels.  Inside a bin each warp takes two balls (one per half-warp): lane hl
-// of a half tests plane zlo + hl of its ball -- the plane needs work only if
-// some open row in the disk's y-range has an unpainted voxel inside the disk's
+// voxels.  A bin is processed in rounds of up to kRound balls, each in two
+// phases.  Test: each warp takes two balls (one per half-warp); lane hl of a
+// half tests plane zlo + hl of its ball -- the plane needs work only if some
+// open row in the disk's y-range has an unpainted voxel inside the disk's
 // widest chord (a stale range-OR table is a superset, so it never skips work)
-// -- and then, plane by plane, all 32 lanes take one row each and paint the
-// chord's unpainted voxels.  Non-selected voxels are left 0 here; the site
-// pass adds the ones a sphere reaches.
+// -- and appends the planes that pass to the item list.  Paint: the warps
+// share the items evenly; for an item all 32 lanes take one row each and
+// paint the chord's unpainted voxels.  Balls of one bin have the same r^2, so
+// the order of their items does not matter.  Non-selected voxels are left 0
+// here; the site pass adds the ones a sphere reaches.
 __global__ void __launch_bounds__(kFillThreads, 4)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
                  const uint32_t* __restrict__ rvals, const uint4* __restrict__ rgeo, const FillInfo* __restrict__ info,
@@ -263,18 +268,21 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
   extern __shared__ uint32_t smem[];
   uint16_t* val = reinterpret_cast<uint16_t*>(smem);       // kRows * 32 half-words
   uint32_t* usel = smem + kRows * 16;                        // kRows
-  uint32_t* pln = usel + kRows;                              // kFillTZ
-  uint32_t* boff = pln + kFillTZ;                            // kBinChunk + 1
+  uint32_t* boff = usel + kRows;                             // kBinChunk + 1
   uint32_t* nzb = boff + kBinChunk + 4;                      // kBinChunk
   uint32_t* ent = nzb + kBinChunk;                           // kEntWin
   uint32_t* rot = ent + kEntWin;                             // (kRotLevels - 1) * kFillTZ * 32
+  uint32_t* item = rot + (kRotLevels - 1) * kFillTZ * 32;    // kItems
   __shared__ uint32_t s_nnz, s_wlo, s_whi;
+  __shared__ uint32_t s_nitem[2];
   __shared__ uint32_t wcnt[kFillWarps];
   const uint32_t nR = info->nR;
   const int nw = dm.nw();
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int hl = lane & 15, half = lane >> 4;
+  const unsigned lanes_below = (1u << lane) - 1u;
+  uint32_t parity = 0;  // which item counter the next round uses
   for (long long tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x) {
     const int tx = (int)(tile % g.ntx);
     const int ty = (int)((tile / g.ntx) % g.nty);
@@ -292,18 +300,18 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       continue;
     }
     for (int i = tid; i < kRows * 16; i += kFillThreads) smem[i] = 0u;
-    if (tid < kFillTZ) pln[tid] = 0u;
     if (tid == 0) {
       s_wlo = 0u;
       s_whi = 0u;
+      s_nitem[0] = 0u;
+      s_nitem[1] = 0u;
     }
-    __syncthreads();
+    parity = 0;
     for (int r = tid; r < kRows; r += kFillThreads) {
       const int zz = r / kFillTY, yy = r % kFillTY;
       uint32_t own = 0u;
       if (zz < vz && yy < vy) own = selbits[((long long)(z0 + zz) * dm.h + (y0 + yy)) * nw + tx] & xmask;
       usel[r] = own;
-      if (own) atomicOr(&pln[zz], 1u << yy);
     }
     __syncthreads();
     build_rot(usel, rot, warp, lane, kFillWarps);
@@ -322,7 +330,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
         __syncthreads();
         uint32_t before = 0;
         for (int w = 0; w < warp; ++w) before += wcnt[w];
-        if (ne) nzb[s_nnz + before + __popc(m & ((1u << lane) - 1u))] = i;
+        if (ne) nzb[s_nnz + before + __popc(m & lanes_below)] = i;
         __syncthreads();
         if (tid == 0) {
           uint32_t t = 0;
@@ -335,7 +343,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       for (uint32_t k = 0; k < nnz; ++k) {
         const uint32_t bl = nzb[k];
         const uint4 gq = rgeo[b0 + bl];
-        const uint32_t R = gq.x;
+        const int R = (int)gq.x;
         const uint16_t tag = (uint16_t)(b0 + bl + 1u);
         const int rad = (int)gq.z;                         // isqrt(r2): no lattice point of the ball is further
         const uint32_t e = boff[bl + 1];
@@ -355,19 +363,20 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             }
             __syncthreads();
           }
-          const uint32_t se = min(e, s_whi);
-          const uint32_t* eb = ent + (ss - s_wlo);
-          // two balls per warp: lanes 0..15 test ball 2w, lanes 16..31 ball 2w+1
+          const uint32_t se = min(min(e, s_whi), ss + (uint32_t)kRound);
+          const uint32_t wb = ss - s_wlo;  // window index of the round's first ball
+          // test: two balls per warp, lanes 0..15 on ball 2w, lanes 16..31 on ball 2w+1
           for (uint32_t bp = 2 * warp; bp < se - ss; bp += 2 * kFillWarps) {
             const uint32_t bi = bp + half;
             const bool have = bi < se - ss;
-            const uint32_t c = have ? eb[bi] : 0u;
+            const uint32_t c = have ? ent[wb + bi] : 0u;
             const int cx = (int)(c & 0x3ffu) - 512, cy = (int)((c >> 10) & 0x3ffu) - 512, cz = (int)(c >> 20) - 512;
             const int zlo = max(cz - rad, 0), zhi = min(cz + rad, vz - 1);
+            const int zz = zlo + hl;
             bool pass = false;
-            if (have && zlo + hl <= zhi) {
-              const int zz = zlo + hl, dz = zz - cz;
-              const int prem = (int)R - dz * dz;
+            if (have && zz <= zhi) {
+              const int dz = zz - cz;
+              const int prem = R - dz * dz;
               if (prem >= 0) {
                 const int hy = (int)isqrt24((uint32_t)prem);
                 const int pya = max(cy - hy, 0), pyb = min(cy + hy, vy - 1);
@@ -386,45 +395,50 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
                 }
               }
             }
-            unsigned active = __ballot_sync(0xffffffffu, pass);
-            if (!active) continue;
-            // both balls' centres in every lane (the two halves swap theirs)
-            const uint32_t co = __shfl_xor_sync(0xffffffffu, c, 16);
-            const uint32_t c0 = half ? co : c, c1 = half ? c : co;
-            while (active) {
-              const int k = __ffs(active) - 1;
-              active &= active - 1u;
-              const uint32_t cb = (k & 16) ? c1 : c0;
-              const int bx = (int)(cb & 0x3ffu) - 512, by = (int)((cb >> 10) & 0x3ffu) - 512;
-              const int bz = (int)(cb >> 20) - 512;
-              const int zz = max(bz - rad, 0) + (k & 15);
-              const int dz = zz - bz, dy = lane - by;
-              const int t = (int)R - dz * dz - dy * dy;  // lane = row y of plane zz
-              if (t >= 0) {
-                const int row = zz * kFillTY + lane;
-                const uint32_t m = usel[row];
-                if (m) {
-                  const int hx = (int)isqrt24((uint32_t)t);
-                  const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
-                  if (xa <= xb) {
-                    uint32_t bits = m & range_mask(xa, xb);
-                    if (bits) {
-                      const uint32_t old = atomicAnd(&usel[row], ~bits);
-                      if ((old & ~bits) == 0u) atomicAnd(&pln[zz], ~(1u << lane));
-                      while (bits) {
-                        const int xx = __ffs(bits) - 1;
-                        val[vidx(row, xx)] = tag;
-                        bits &= bits - 1u;
-                      }
+            const unsigned active = __ballot_sync(0xffffffffu, pass);
+            if (active) {
+              uint32_t base = 0;
+              if (lane == 0) base = atomicAdd(&s_nitem[parity], (uint32_t)__popc(active));
+              base = __shfl_sync(0xffffffffu, base, 0);
+              if (pass) item[base + __popc(active & lanes_below)] = ((wb + bi) << 4) | (uint32_t)zz;
+            }
+          }
+          __syncthreads();
+          // paint: the round's items over all warps, one row per lane
+          const uint32_t nitem = s_nitem[parity];
+          if (tid == 0) s_nitem[parity ^ 1u] = 0u;  // the next round's counter (idle since the last barrier)
+          for (uint32_t it = warp; it < nitem; it += kFillWarps) {
+            const uint32_t q = item[it];
+            const int zz = (int)(q & 15u);
+            const uint32_t cb = ent[q >> 4];
+            const int bx = (int)(cb & 0x3ffu) - 512, by = (int)((cb >> 10) & 0x3ffu) - 512;
+            const int bz = (int)(cb >> 20) - 512;
+            const int dz = zz - bz, dy = lane - by;
+            const int t = R - dz * dz - dy * dy;  // lane = row y of plane zz
+            if (t >= 0) {
+              const int row = zz * kFillTY + lane;
+              const uint32_t m = usel[row];
+              if (m) {
+                const int hx = (int)isqrt24((uint32_t)t);
+                const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
+                if (xa <= xb) {
+                  uint32_t bits = m & range_mask(xa, xb);
+                  if (bits) {
+                    atomicAnd(&usel[row], ~bits);
+                    while (bits) {
+                      const int xx = __ffs(bits) - 1;
+                      val[vidx(row, xx)] = tag;
+                      bits &= bits - 1u;
                     }
                   }
                 }
               }
             }
           }
+          parity ^= 1u;
+          __syncthreads();
           ss = se;
         }
-        __syncthreads();
         if (k % kRotEvery == kRotEvery - 1) {
           build_rot(usel, rot, warp, lane, kFillWarps);
           __syncthreads();
