@@ -5,6 +5,20 @@
 
 namespace bm {
 
+// Grid of a persistent (tile-looping) kernel: as many CTAs as the current
+// device keeps resident at once, at most one per tile.
+template <typename Kernel>
+inline unsigned resident_grid(Kernel kernel, int threads, size_t smem, long long tiles) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
+  long long g = (long long)(per > 0 ? per : 1) * (sms > 0 ? sms : 1);
+  if (g > tiles) g = tiles;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
 // Bytes of device scratch the EDT line passes need for a volume.
 size_t edt_scratch_bytes(Dims dm);
 

@@ -124,6 +124,16 @@ constexpr int kCSZ = kCTZ + 2 * kCH;         // 12
 constexpr uint32_t kOob = 0xffffffffu;
 constexpr int kCleanThreads = 256;
 
+__device__ __forceinline__ void flush_run(StatsAccum& sacc, uint32_t e, unsigned long long& s1,
+                                          unsigned long long& sh, unsigned long long& sl) {
+  if (s1) {
+    atomicAdd(&sacc.sum_m[e], s1);
+    atomicAdd(&sacc.sq_hi[e], sh);
+    atomicAdd(&sacc.sq_lo[e], sl);
+    s1 = sh = sl = 0;
+  }
+}
+
 __global__ void __launch_bounds__(kCleanThreads)
 cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict__ selbits, Dims dm,
                     const float* __restrict__ dia, float scale, float* __restrict__ outmap,
@@ -146,6 +156,11 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
   const int nw = dm.nw();
   unsigned long long cnt = 0;
   uint32_t mx = 0;
+  // this thread's run of values with one f32 exponent: sums of the mantissas
+  // and of the two 24-bit halves of their squares (flushed when the exponent
+  // changes, so a thread's values are added once, without warp votes)
+  uint32_t run_e = 0;
+  unsigned long long run_s1 = 0, run_sh = 0, run_sl = 0;
   const long long ntiles = (long long)ntx * nty * ntz;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
@@ -199,10 +214,15 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
       const int oz = r / kCTY, oy = r % kCTY;
       const int z = z0 + oz, y = y0 + oy, x = x0 + lane;
       if (z >= dm.d || y >= dm.h) continue;
+      const uint32_t selw = selbits[((long long)z * dm.h + y) * nw + tx];
+      float* orow = outmap ? outmap + ((long long)z * dm.h + y) * dm.w : nullptr;
+      if (selw == 0u) {  // nothing selected in this row: the masked map is 0
+        if (orow && x < dm.w) orow[x] = 0.0f;
+        continue;
+      }
       const int sz = oz + kCH, sy = oy + kCH, sx = lane + kCH;
       float val = 0.0f;
-      const bool sel = x < dm.w && ((selbits[((long long)z * dm.h + y) * nw + tx] >> lane) & 1u);
-      if (sel) {
+      if (x < dm.w && ((selw >> lane) & 1u)) {
         const uint32_t t = T[(sz * kCSY + sy) * kCSX + sx];
         if (t != 0u) {
           const float own = __uint_as_float(t);
@@ -232,30 +252,26 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
           }
         }
       }
-      if (outmap && x < dm.w) outmap[((long long)z * dm.h + y) * dm.w + x] = val;
-      const unsigned pos = __ballot_sync(0xffffffffu, val > 0.0f);
+      if (orow && x < dm.w) orow[x] = val;
       if (val > 0.0f) {
-        const float v = __fmul_rn(val, scale);
+        const uint32_t bits = __float_as_uint(__fmul_rn(val, scale));
         ++cnt;
-        mx = max(mx, __float_as_uint(v));
-        // lanes holding the same exponent add their mantissa sums in one step
-        const uint32_t bits = __float_as_uint(v);
+        mx = max(mx, bits);
         uint32_t e = bits >> 23, m = bits & 0x7fffffu;
         if (e) m |= 0x800000u;
         else e = 1;
-        const unsigned long long sq = (unsigned long long)m * m;
-        const unsigned grp = __match_any_sync(pos, e);
-        const uint32_t s1 = __reduce_add_sync(grp, m);
-        const uint32_t sh = __reduce_add_sync(grp, (uint32_t)(sq >> 24));
-        const uint32_t sl = __reduce_add_sync(grp, (uint32_t)(sq & 0xffffffu));
-        if (lane == __ffs(grp) - 1) {
-          atomicAdd(&sacc.sum_m[e], (unsigned long long)s1);
-          atomicAdd(&sacc.sq_hi[e], (unsigned long long)sh);
-          atomicAdd(&sacc.sq_lo[e], (unsigned long long)sl);
+        if (e != run_e) {  // a new exponent: flush this thread's run
+          flush_run(sacc, run_e, run_s1, run_sh, run_sl);
+          run_e = e;
         }
+        const unsigned long long sq = (unsigned long long)m * m;
+        run_s1 += m;
+        run_sh += sq >> 24;
+        run_sl += sq & 0xffffffu;
       }
     }
   }
+  flush_run(sacc, run_e, run_s1, run_sh, run_sl);
   if (cnt) atomicAdd(&sacc.count, cnt);
   if (mx) atomicMax(&sacc.max_bits, mx);
   __syncthreads();
@@ -397,8 +413,8 @@ cudaError_t launch_ridges(const uint32_t* dist, Dims dm, const uint4* lut, uint2
                           uint32_t* occ, cudaStream_t s, unsigned long long* launches) {
   const int ntx = (dm.w + kRTX - 1) / kRTX, nty = (dm.h + kRTY - 1) / kRTY, ntz = (dm.d + kRTZ - 1) / kRTZ;
   const long long tiles = (long long)ntx * nty * ntz;
-  ridge_tile_kernel<<<(unsigned)(tiles < 152 * 8 ? tiles : 152 * 8), 256, 0, s>>>(dist, dm, lut, ridges, ctr, occ, ntx,
-                                                                                 nty, ntz);
+  ridge_tile_kernel<<<resident_grid(ridge_tile_kernel, 256, 0, tiles), 256, 0, s>>>(dist, dm, lut, ridges, ctr, occ,
+                                                                                    ntx, nty, ntz);
   ++*launches;
   return cudaGetLastError();
 }
@@ -414,7 +430,7 @@ cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dim
                            float* outmap, StatsAccum* acc, cudaStream_t s, unsigned long long* launches) {
   const int ntx = (dm.w + kCTX - 1) / kCTX, nty = (dm.h + kCTY - 1) / kCTY, ntz = (dm.d + kCTZ - 1) / kCTZ;
   const long long tiles = (long long)ntx * nty * ntz;
-  const unsigned grid = (unsigned)(tiles < 152 * 8 ? tiles : 152 * 8);
+  const unsigned grid = resident_grid(cleanup_tile_kernel, kCleanThreads, 0, tiles);
   cleanup_tile_kernel<<<grid, kCleanThreads, 0, s>>>(fillmap, selbits, dm, dia, scale, outmap, acc, ntx, nty, ntz);
   ++*launches;
   return cudaGetLastError();
