@@ -134,6 +134,26 @@ __device__ __forceinline__ void flush_run(StatsAccum& sacc, uint32_t e, unsigned
   }
 }
 
+// One value of the calibrated map into this thread's statistics.
+__device__ __forceinline__ void add_value(float val, float scale, unsigned long long& cnt, uint32_t& mx,
+                                          uint32_t& run_e, unsigned long long& run_s1, unsigned long long& run_sh,
+                                          unsigned long long& run_sl, StatsAccum& sacc) {
+  const uint32_t bits = __float_as_uint(__fmul_rn(val, scale));
+  ++cnt;
+  mx = max(mx, bits);
+  uint32_t e = bits >> 23, m = bits & 0x7fffffu;
+  if (e) m |= 0x800000u;
+  else e = 1;
+  if (e != run_e) {  // a new exponent: flush this thread's run
+    flush_run(sacc, run_e, run_s1, run_sh, run_sl);
+    run_e = e;
+  }
+  const unsigned long long sq = (unsigned long long)m * m;
+  run_s1 += m;
+  run_sh += sq >> 24;
+  run_sl += sq & 0xffffffu;
+}
+
 __global__ void __launch_bounds__(kCleanThreads)
 cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict__ selbits, Dims dm,
                     const float* __restrict__ dia, float scale, float* __restrict__ outmap,
@@ -166,29 +186,40 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
     const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
     const int x0 = tx * kCTX, y0 = ty * kCTY, z0 = tz * kCTZ;
     __syncthreads();
-    // stage the r^2 map with halo 2: one row of 36 per warp step
-    for (int r = warp; r < kCSZ * kCSY; r += kCleanThreads / 32) {
-      const int z = z0 - kCH + r / kCSY, y = y0 - kCH + r % kCSY;
-      const bool rin = z >= 0 && z < dm.d && y >= 0 && y < dm.h;
-      const uint32_t* row = fm + ((long long)z * dm.h + y) * dm.w;
-      uint32_t* srow = T + r * kCSX;
-      int x = x0 - kCH + lane;
-      uint32_t v = (rin && x >= 0 && x < dm.w) ? row[x] : kOob;
-      // staged as the f32 diameter bits (2*sqrt(r^2)); 0 stays 0
-      srow[lane] = (v == 0u || v == kOob) ? 0u : __float_as_uint(dia[v]);
-      unsigned b = __ballot_sync(0xffffffffu, v != 0u);
-      uint32_t v2 = kOob;
-      if (lane < kCSX - 32) {
-        x = x0 - kCH + 32 + lane;
-        v2 = (rin && x < dm.w) ? row[x] : kOob;
-        srow[32 + lane] = (v2 == 0u || v2 == kOob) ? 0u : __float_as_uint(dia[v2]);
+    // stage the r^2 map with halo 2: one row of 36 per warp step.  Each warp
+    // has 18 rows; their loads are issued in batches of 3 before any use, so
+    // the latencies overlap.
+    constexpr int kRowsPerWarp = kCSZ * kCSY / (kCleanThreads / 32);  // 18
+    constexpr int kBatch = 3;
+    static_assert(kCSZ * kCSY % (kCleanThreads / 32) == 0 && kRowsPerWarp % kBatch == 0, "staging split");
+#pragma unroll
+    for (int b = 0; b < kRowsPerWarp; b += kBatch) {
+      uint32_t v[kBatch], v2[kBatch];
+#pragma unroll
+      for (int j = 0; j < kBatch; ++j) {
+        const int r = warp + (kCleanThreads / 32) * (b + j);
+        const int z = z0 - kCH + r / kCSY, y = y0 - kCH + r % kCSY;
+        const bool rin = z >= 0 && z < dm.d && y >= 0 && y < dm.h;
+        const uint32_t* row = fm + ((long long)z * dm.h + y) * dm.w;
+        const int x = x0 - kCH + lane, xb = x0 - kCH + 32 + lane;
+        v[j] = (rin && x >= 0 && x < dm.w) ? row[x] : kOob;
+        v2[j] = (lane < kCSX - 32 && rin && xb < dm.w) ? row[xb] : kOob;
       }
-      const unsigned b2 = __ballot_sync(0xffffffffu, lane < kCSX - 32 && v2 != 0u);
-      const unsigned o1 = __ballot_sync(0xffffffffu, v != 0u && v != kOob);
-      const unsigned o2 = __ballot_sync(0xffffffffu, lane < kCSX - 32 && v2 != 0u && v2 != kOob);
-      if (lane == 0) {
-        nz[r] = (unsigned long long)b | ((unsigned long long)b2 << 32);
-        own[r] = (unsigned long long)o1 | ((unsigned long long)o2 << 32);
+#pragma unroll
+      for (int j = 0; j < kBatch; ++j) {
+        const int r = warp + (kCleanThreads / 32) * (b + j);
+        uint32_t* srow = T + r * kCSX;
+        // staged as the f32 diameter bits (2*sqrt(r^2)); 0 stays 0
+        srow[lane] = (v[j] == 0u || v[j] == kOob) ? 0u : __float_as_uint(dia[v[j]]);
+        if (lane < kCSX - 32) srow[32 + lane] = (v2[j] == 0u || v2[j] == kOob) ? 0u : __float_as_uint(dia[v2[j]]);
+        const unsigned b1 = __ballot_sync(0xffffffffu, v[j] != 0u);
+        const unsigned b2 = __ballot_sync(0xffffffffu, lane < kCSX - 32 && v2[j] != 0u);
+        const unsigned o1 = __ballot_sync(0xffffffffu, v[j] != 0u && v[j] != kOob);
+        const unsigned o2 = __ballot_sync(0xffffffffu, lane < kCSX - 32 && v2[j] != 0u && v2[j] != kOob);
+        if (lane == 0) {
+          nz[r] = (unsigned long long)b1 | ((unsigned long long)b2 << 32);
+          own[r] = (unsigned long long)o1 | ((unsigned long long)o2 << 32);
+        }
       }
     }
     __syncthreads();
@@ -253,22 +284,7 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
         }
       }
       if (orow && x < dm.w) orow[x] = val;
-      if (val > 0.0f) {
-        const uint32_t bits = __float_as_uint(__fmul_rn(val, scale));
-        ++cnt;
-        mx = max(mx, bits);
-        uint32_t e = bits >> 23, m = bits & 0x7fffffu;
-        if (e) m |= 0x800000u;
-        else e = 1;
-        if (e != run_e) {  // a new exponent: flush this thread's run
-          flush_run(sacc, run_e, run_s1, run_sh, run_sl);
-          run_e = e;
-        }
-        const unsigned long long sq = (unsigned long long)m * m;
-        run_s1 += m;
-        run_sh += sq >> 24;
-        run_sl += sq & 0xffffffu;
-      }
+      if (val > 0.0f) add_value(val, scale, cnt, mx, run_e, run_s1, run_sh, run_sl, sacc);
     }
   }
   flush_run(sacc, run_e, run_s1, run_sh, run_sl);
@@ -307,16 +323,31 @@ ridge_tile_kernel(const uint32_t* __restrict__ dist, Dims dm, const uint4* __res
     const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
     const int x0 = tx * kRTX, y0 = ty * kRTY, z0 = tz * kRTZ;
     __syncthreads();
-    for (int r = warp; r < kRSZ * kRSY; r += 8) {
-      const int z = z0 - 1 + r / kRSY, y = y0 - 1 + r % kRSY;
-      const bool rin = z >= 0 && z < dm.d && y >= 0 && y < dm.h;
-      const uint32_t* row = dist + ((long long)z * dm.h + y) * dm.w;
-      uint32_t* srow = D + r * kRSX;
-      int x = x0 - 1 + lane;
-      srow[lane] = (rin && x >= 0 && x < dm.w) ? row[x] : 0u;
-      if (lane < 2) {
-        x = x0 + 31 + lane;
-        srow[32 + lane] = (rin && x < dm.w) ? row[x] : 0u;
+    // stage the distance map with halo 1: one row of 34 per warp step, loads
+    // of all the warp's rows issued before the stores
+    constexpr int kRidgeRows = (kRSZ * kRSY + 7) / 8;  // 13 (the last step covers 4 rows)
+    constexpr int kRBatch = 5;
+#pragma unroll
+    for (int b = 0; b < kRidgeRows; b += kRBatch) {
+      uint32_t v[kRBatch], v2[kRBatch];
+#pragma unroll
+      for (int j = 0; j < kRBatch; ++j) {
+        const int r = warp + 8 * (b + j);
+        const int z = z0 - 1 + r / kRSY, y = y0 - 1 + r % kRSY;
+        const bool rin = b + j < kRidgeRows && r < kRSZ * kRSY && z >= 0 && z < dm.d && y >= 0 && y < dm.h;
+        const uint32_t* row = dist + ((long long)z * dm.h + y) * dm.w;
+        const int x = x0 - 1 + lane, xb = x0 + 31 + lane;
+        v[j] = (rin && x >= 0 && x < dm.w) ? row[x] : 0u;
+        v2[j] = (lane < 2 && rin && xb < dm.w) ? row[xb] : 0u;
+      }
+#pragma unroll
+      for (int j = 0; j < kRBatch; ++j) {
+        const int r = warp + 8 * (b + j);
+        if (b + j < kRidgeRows && r < kRSZ * kRSY) {
+          uint32_t* srow = D + r * kRSX;
+          srow[lane] = v[j];
+          if (lane < 2) srow[32 + lane] = v2[j];
+        }
       }
     }
     __syncthreads();
