@@ -374,12 +374,14 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             const int zlo = max(cz - rad, 0), zhi = min(cz + rad, vz - 1);
             const int zz = zlo + hl;
             bool pass = false;
+            int pya = 0, pyb = 0;  // the disk's rows inside the tile
             if (have && zz <= zhi) {
               const int dz = zz - cz;
               const int prem = R - dz * dz;
               if (prem >= 0) {
                 const int hy = (int)isqrt24((uint32_t)prem);
-                const int pya = max(cy - hy, 0), pyb = min(cy + hy, vy - 1);
+                pya = max(cy - hy, 0);
+                pyb = min(cy + hy, vy - 1);
                 const int xa = max(cx - hy, 0), xb = min(cx + hy, vx - 1);
                 if (pya <= pyb && xa <= xb) {
                   const int span = pyb - pya + 1;
@@ -395,46 +397,54 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
                 }
               }
             }
-            const unsigned active = __ballot_sync(0xffffffffu, pass);
-            if (active) {
+            // items: (window index, rows ya .. ya + n - 1, plane); planes of at
+            // most 16 rows go to the half-warp list at the top of the array
+            const bool wide = pass && pyb - pya >= 16;
+            const unsigned act_w = __ballot_sync(0xffffffffu, wide);
+            const unsigned act_n = __ballot_sync(0xffffffffu, pass && !wide);
+            if (act_w | act_n) {
               uint32_t base = 0;
-              if (lane == 0) base = atomicAdd(&s_nitem[parity], (uint32_t)__popc(active));
+              if (lane == 0) base = atomicAdd(&s_nitem[parity], (uint32_t)__popc(act_w) | ((uint32_t)__popc(act_n) << 16));
               base = __shfl_sync(0xffffffffu, base, 0);
-              if (pass) item[base + __popc(active & lanes_below)] = ((wb + bi) << 4) | (uint32_t)zz;
+              const uint32_t q = ((wb + bi) << 14) | ((uint32_t)(pyb - pya) << 9) | ((uint32_t)pya << 4) | (uint32_t)zz;
+              if (wide) item[(base & 0xffffu) + __popc(act_w & lanes_below)] = q;
+              else if (pass) item[kItems - 1 - ((base >> 16) + __popc(act_n & lanes_below))] = q;
             }
           }
           __syncthreads();
-          // paint: the round's items over all warps, one row per lane
-          const uint32_t nitem = s_nitem[parity];
+          // paint: the round's items over all warps, one row per lane (wide
+          // planes) or per half-warp lane (planes of at most 16 rows)
+          const uint32_t packed = s_nitem[parity];
           if (tid == 0) s_nitem[parity ^ 1u] = 0u;  // the next round's counter (idle since the last barrier)
-          for (uint32_t it = warp; it < nitem; it += kFillWarps) {
-            const uint32_t q = item[it];
-            const int zz = (int)(q & 15u);
-            const uint32_t cb = ent[q >> 4];
+          const uint32_t nwide = packed & 0xffffu, nnarrow = packed >> 16;
+          auto paint_row = [&](uint32_t q, int j) {  // row ya + j of item q
+            const int zz = (int)(q & 15u), ya = (int)((q >> 4) & 31u);
+            if (j > (int)((q >> 9) & 31u)) return;
+            const int y = ya + j;
+            const uint32_t cb = ent[q >> 14];
             const int bx = (int)(cb & 0x3ffu) - 512, by = (int)((cb >> 10) & 0x3ffu) - 512;
             const int bz = (int)(cb >> 20) - 512;
-            const int dz = zz - bz, dy = lane - by;
-            const int t = R - dz * dz - dy * dy;  // lane = row y of plane zz
-            if (t >= 0) {
-              const int row = zz * kFillTY + lane;
-              const uint32_t m = usel[row];
-              if (m) {
-                const int hx = (int)isqrt24((uint32_t)t);
-                const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
-                if (xa <= xb) {
-                  uint32_t bits = m & range_mask(xa, xb);
-                  if (bits) {
-                    atomicAnd(&usel[row], ~bits);
-                    while (bits) {
-                      const int xx = __ffs(bits) - 1;
-                      val[vidx(row, xx)] = tag;
-                      bits &= bits - 1u;
-                    }
-                  }
-                }
-              }
+            const int dz = zz - bz, dy = y - by;
+            const int t = R - dz * dz - dy * dy;
+            if (t < 0) return;
+            const int row = zz * kFillTY + y;
+            const uint32_t m = usel[row];
+            if (!m) return;
+            const int hx = (int)isqrt24((uint32_t)t);
+            const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
+            if (xa > xb) return;
+            uint32_t bits = m & range_mask(xa, xb);
+            if (!bits) return;
+            atomicAnd(&usel[row], ~bits);
+            while (bits) {
+              const int xx = __ffs(bits) - 1;
+              val[vidx(row, xx)] = tag;
+              bits &= bits - 1u;
             }
-          }
+          };
+          for (uint32_t it = warp; it < nwide; it += kFillWarps) paint_row(item[it], lane);
+          for (uint32_t it = 2 * warp + half; it < ((nnarrow + 1u) & ~1u); it += 2 * kFillWarps)
+            if (it < nnarrow) paint_row(item[kItems - 1 - it], hl);
           parity ^= 1u;
           __syncthreads();
           ss = se;
