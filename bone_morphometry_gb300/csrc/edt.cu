@@ -11,6 +11,7 @@
 //            intersection test done by int64 cross-multiplication; lines
 //            whose every entry is "no site" (kInfSq) stay kInfSq.
 #include <climits>
+#include <cstdint>
 
 #include "kernels.h"
 
@@ -58,6 +59,130 @@ edt_x_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, Dims 
         mask[c] = site;
         selbits[row * nw + c] = selw;
         sites += __popc(site);
+      }
+    }
+    __syncwarp();
+    int carry = -1;
+    for (int c0 = 0; c0 < nw; c0 += 32) {
+      const int c = c0 + lane;
+      int v = (c < nw && mask[c] != 0u) ? c : -1;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v = max(v, t);
+      }
+      v = max(v, carry);
+      if (c < nw) prevnz[c] = v;
+      carry = __shfl_sync(0xffffffffu, v, 31);
+    }
+    carry = INT_MAX;
+    for (int c0 = ((nw - 1) >> 5) << 5; c0 >= 0; c0 -= 32) {
+      const int c = c0 + lane;
+      int v = (c < nw && mask[c] != 0u) ? c : INT_MAX;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_down_sync(0xffffffffu, v, o);
+        if (lane + o < 32) v = min(v, t);
+      }
+      v = min(v, carry);
+      if (c < nw) nextnz[c] = v;
+      carry = __shfl_sync(0xffffffffu, v, 0);
+    }
+    __syncwarp();
+    for (int c = 0; c < nw; ++c) {
+      const int x = c * 32 + lane;
+      if (x < dm.w) {
+        const uint32_t m = mask[c];
+        uint32_t val = 0;
+        if (!((m >> lane) & 1u)) {
+          int left = -1, right = -1;
+          const uint32_t lo = m & ((1u << lane) - 1u);
+          if (lo) {
+            left = c * 32 + 31 - __clz(lo);
+          } else if (c > 0) {
+            const int p = prevnz[c - 1];
+            if (p >= 0) left = p * 32 + 31 - __clz(mask[p]);
+          }
+          const uint32_t hi = (lane == 31) ? 0u : (m & ~((2u << lane) - 1u));
+          if (hi) {
+            right = c * 32 + __ffs(hi) - 1;
+          } else if (c + 1 < nw) {
+            const int p = nextnz[c + 1];
+            if (p != INT_MAX) right = p * 32 + __ffs(mask[p]) - 1;
+          }
+          int g = INT_MAX;
+          if (left >= 0) g = x - left;
+          if (right >= 0) g = min(g, right - x);
+          val = (g == INT_MAX) ? kInfSq : (uint32_t)g * (uint32_t)g;
+        }
+        out[base + x] = val;
+      }
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && sites) atomicAdd(&ctr->sites, sites);
+}
+
+// 4-bit selection mask of the 4 voxels in a (bone) and b (roi) words:
+// per byte, the MODE predicate, packed to bits 0..3.
+template <int MODE>
+__device__ __forceinline__ uint32_t sel4(uint32_t a, uint32_t b) {
+  const uint32_t nza = __vcmpne4(a, 0u), nzb = __vcmpne4(b, 0u);  // 0xff per nonzero byte
+  uint32_t m;
+  if (MODE == SEL_FOREGROUND) m = nza;
+  else if (MODE == SEL_BACKGROUND) m = ~nza;
+  else if (MODE == SEL_BONE_IN_ROI) m = nzb & nza;
+  else m = nzb & ~nza;
+  m &= 0x01010101u;
+  return (m * 0x01020408u) >> 24 & 0xfu;  // bytes 0..3 -> bits 0..3
+}
+
+// The x pass for rows whose bytes are 16-byte aligned (w a multiple of 16 and
+// aligned inputs): each lane loads 16 voxels of bone and roi at once and the
+// lanes' 16-bit masks pair up into the row's 32-bit words; the distances are
+// then computed as in edt_x_kernel, one x per lane (coalesced stores).
+template <int MODE>
+__global__ void __launch_bounds__(kXWarps * 32)
+edt_x_vec_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, Dims dm, uint32_t* __restrict__ out,
+                 uint32_t* __restrict__ selbits, Counters* __restrict__ ctr) {
+  extern __shared__ uint32_t smem[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nw = dm.nw();
+  uint32_t* mask = smem + (size_t)warp * 3 * nw;
+  int* prevnz = reinterpret_cast<int*>(mask + nw);
+  int* nextnz = prevnz + nw;
+  const long long rows = (long long)dm.h * dm.d;
+  const bool two = MODE == SEL_BONE_IN_ROI || MODE == SEL_MARROW_IN_ROI;
+  unsigned long long sites = 0;
+
+  for (long long row = (long long)blockIdx.x * kXWarps + warp; row < rows;
+       row += (long long)gridDim.x * kXWarps) {
+    const long long base = row * dm.w;
+    const uint4* av = reinterpret_cast<const uint4*>(a + base);
+    const uint4* bv = two ? reinterpret_cast<const uint4*>(b + base) : nullptr;
+    const int nvec = dm.w >> 4;  // 16 voxels per uint4
+    for (int v0 = 0; v0 < nvec; v0 += 32) {
+      const int v = v0 + lane;
+      uint32_t s16 = 0, t16 = 0;
+      if (v < nvec) {
+        const uint4 A = av[v];
+        const uint4 B = two ? bv[v] : make_uint4(0u, 0u, 0u, 0u);
+        s16 = sel4<MODE>(A.x, B.x) | (sel4<MODE>(A.y, B.y) << 4) | (sel4<MODE>(A.z, B.z) << 8) |
+              (sel4<MODE>(A.w, B.w) << 12);
+        t16 = ~s16 & 0xffffu;  // all 16 voxels lie inside the row
+      }
+      const uint32_t s_hi = __shfl_down_sync(0xffffffffu, s16, 1);
+      const uint32_t t_hi = __shfl_down_sync(0xffffffffu, t16, 1);
+      if (!(lane & 1) && v < nvec) {
+        const int c = v >> 1;  // word index: voxels 32c .. 32c + 31
+        // a row of 16k voxels with k odd ends on a half word: its upper half is empty
+        const bool full = v + 1 < nvec;
+        const uint32_t sw = s16 | (full ? s_hi << 16 : 0u);
+        const uint32_t tw = t16 | (full ? t_hi << 16 : 0u);
+        mask[c] = tw;
+        selbits[row * nw + c] = sw;
+        sites += __popc(tw);
       }
     }
     __syncwarp();
@@ -211,6 +336,17 @@ constexpr int kWinTL = 128;
 constexpr int kWinHalo = 64;
 constexpr int kWinThreads = 256;
 constexpr int kWinWarps = kWinThreads / 32;
+// "No site" inside the window kernel: larger than any real squared distance
+// (< 2^30 + 2^30) yet small enough that adding a staged offset dp^2 (dp <=
+// kWinHalo + 3) cannot wrap, so the scan needs no special case for it.
+constexpr uint32_t kBigSq = 0xF0000000u;
+
+// floor(sqrt(f)) + 2 >= isqrt(f - 1) + 1 for f >= 1: the halo that f needs,
+// from the hardware reciprocal square root (error far below one).
+__device__ __forceinline__ uint32_t halo_need(uint32_t f) {
+  const float ff = (float)f;
+  return (uint32_t)(ff * rsqrtf(ff)) + 2u;
+}
 
 __global__ void __launch_bounds__(kWinThreads)
 edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int n, long long stride, int w,
@@ -229,17 +365,20 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
   const int q0 = chunk * kWinTL;
   if (threadIdx.x == 0) s_need = 0u;
   __syncthreads();
-  // centre rows
+  // centre rows (loads of the warp's 16 rows issued before their use)
   uint32_t need = 0;
-  for (int i = warp; i < kWinTL; i += kWinWarps) {
-    const int q = q0 + i;
-    uint32_t f = kInfSq;
-    if (xin && q < n) {
-      f = in[base + (long long)q * stride];
-      const uint32_t nd = (f == 0u) ? 0u : (f == kInfSq ? 0xffffu : (uint32_t)sqrtf((float)(f - 1u)) + 1u);
-      need = max(need, nd);
-    }
-    buf[(kWinHalo + i) * 32 + lane] = f;
+  constexpr int kPer = kWinTL / kWinWarps;  // 16
+  uint32_t f[kPer];
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int q = q0 + warp + kWinWarps * j;
+    f[j] = (xin && q < n) ? in[base + (long long)q * stride] : kInfSq;
+  }
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const uint32_t v = f[j];
+    if (v != 0u) need = max(need, v == kInfSq ? 0xffffu : halo_need(v));
+    buf[(kWinHalo + warp + kWinWarps * j) * 32 + lane] = v == kInfSq ? kBigSq : v;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
@@ -248,13 +387,17 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
   const int halo = (int)min(s_need, (uint32_t)kWinHalo);
   for (int i = warp; i < halo; i += kWinWarps) {
     const int ql = q0 - 1 - i, qr = q0 + kWinTL + i;
-    buf[(kWinHalo - 1 - i) * 32 + lane] = (xin && ql >= 0) ? in[base + (long long)ql * stride] : kInfSq;
-    buf[(kWinHalo + kWinTL + i) * 32 + lane] = (xin && qr < n) ? in[base + (long long)qr * stride] : kInfSq;
+    const uint32_t l = (xin && ql >= 0) ? in[base + (long long)ql * stride] : kInfSq;
+    const uint32_t r = (xin && qr < n) ? in[base + (long long)qr * stride] : kInfSq;
+    buf[(kWinHalo - 1 - i) * 32 + lane] = l == kInfSq ? kBigSq : l;
+    buf[(kWinHalo + kWinTL + i) * 32 + lane] = r == kInfSq ? kBigSq : r;
   }
   __syncthreads();
   uint32_t localmax = 0;
   bool bad = false;
-  for (int i = warp; i < kWinTL; i += kWinWarps) {
+#pragma unroll 1
+  for (int j = 0; j < kPer; ++j) {
+    const int i = warp + kWinWarps * j;
     const int q = q0 + i;
     if (!xin || q >= n) continue;
     const uint32_t* col = buf + (kWinHalo + i) * 32 + lane;
@@ -263,17 +406,27 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
       out[base + (long long)q * stride] = 0u;
       continue;
     }
-    // every p with |q - p| < dp has been tried once dp^2 >= best; if the scan
-    // would have to pass the staged halo first, the line is redone exactly
+    // every p with |q - p| < dp has been tried once dp^2 >= best (a step
+    // with dp^2 >= best cannot lower it, so four steps run at a time); if the
+    // scan would have to pass the staged halo, the line is redone exactly
     bool done = true;
-    for (int dp = 1; (uint32_t)(dp * dp) < best; ++dp) {
-      if (dp > halo) {
-        done = false;
-        break;
+    int dp = 1;
+    while ((uint32_t)(dp * dp) < best) {
+      if (dp + 3 <= halo) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int d = dp + u;
+          best = min(best, min(col[-d * 32], col[d * 32]) + (uint32_t)(d * d));
+        }
+        dp += 4;
+      } else {
+        if (dp > halo) {
+          done = false;
+          break;
+        }
+        best = min(best, min(col[-dp * 32], col[dp * 32]) + (uint32_t)(dp * dp));
+        ++dp;
       }
-      const uint32_t a = col[-dp * 32], b = col[dp * 32];
-      const uint32_t c = min(a, b);
-      if (c != kInfSq) best = min(best, c + (uint32_t)(dp * dp));
     }
     if (!done) {
       bad = true;
@@ -298,47 +451,51 @@ size_t edt_scratch_bytes(Dims dm) {
   return (size_t)y_pass * 2 * sizeof(uint32_t);
 }
 
+template <int MODE>
+cudaError_t launch_edt_x_mode(const uint8_t* a, const uint8_t* b, Dims dm, uint32_t* out, uint32_t* selbits,
+                              Counters* ctr, unsigned blocks, size_t smem, cudaStream_t s) {
+  const bool two = MODE == SEL_BONE_IN_ROI || MODE == SEL_MARROW_IN_ROI;
+  const bool vec = dm.w % 16 == 0 && (reinterpret_cast<uintptr_t>(a) & 15u) == 0 &&
+                   (!two || (reinterpret_cast<uintptr_t>(b) & 15u) == 0);
+  if (vec) {
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(edt_x_vec_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    edt_x_vec_kernel<MODE><<<blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+  } else {
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(edt_x_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    edt_x_kernel<MODE><<<blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_edt_x(const uint8_t* a, const uint8_t* b, int mode, Dims dm, uint32_t* out,
                          uint32_t* selbits, Counters* ctr, cudaStream_t s, unsigned long long* launches) {
   const long long rows = (long long)dm.h * dm.d;
   long long blocks = (rows + kXWarps - 1) / kXWarps;
   if (blocks > 152 * 64) blocks = 152 * 64;
   const size_t smem = (size_t)kXWarps * 3 * dm.nw() * sizeof(uint32_t);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaSuccess;
-    switch (mode) {
-      case SEL_FOREGROUND:
-        e = cudaFuncSetAttribute(edt_x_kernel<SEL_FOREGROUND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        break;
-      case SEL_BACKGROUND:
-        e = cudaFuncSetAttribute(edt_x_kernel<SEL_BACKGROUND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        break;
-      case SEL_BONE_IN_ROI:
-        e = cudaFuncSetAttribute(edt_x_kernel<SEL_BONE_IN_ROI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        break;
-      default:
-        e = cudaFuncSetAttribute(edt_x_kernel<SEL_MARROW_IN_ROI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        break;
-    }
-    if (e != cudaSuccess) return e;
-  }
+  cudaError_t e;
   switch (mode) {
     case SEL_FOREGROUND:
-      edt_x_kernel<SEL_FOREGROUND><<<(unsigned)blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+      e = launch_edt_x_mode<SEL_FOREGROUND>(a, b, dm, out, selbits, ctr, (unsigned)blocks, smem, s);
       break;
     case SEL_BACKGROUND:
-      edt_x_kernel<SEL_BACKGROUND><<<(unsigned)blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+      e = launch_edt_x_mode<SEL_BACKGROUND>(a, b, dm, out, selbits, ctr, (unsigned)blocks, smem, s);
       break;
     case SEL_BONE_IN_ROI:
-      edt_x_kernel<SEL_BONE_IN_ROI><<<(unsigned)blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+      e = launch_edt_x_mode<SEL_BONE_IN_ROI>(a, b, dm, out, selbits, ctr, (unsigned)blocks, smem, s);
       break;
     default:
-      edt_x_kernel<SEL_MARROW_IN_ROI><<<(unsigned)blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);
+      e = launch_edt_x_mode<SEL_MARROW_IN_ROI>(a, b, dm, out, selbits, ctr, (unsigned)blocks, smem, s);
       break;
   }
   ++*launches;
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t launch_edt_line(int axis, const uint32_t* in, uint32_t* out, Dims dm, void* scratch, Counters* ctr,

@@ -40,6 +40,9 @@ EDT_CASES = [
     ((17, 129, 40), 0.97, 5), ((64, 64, 64), 0.5, 6), ((2, 300, 3), 0.99, 7), ((41, 2, 257), 0.8, 8),
     ((16, 16, 1100), 0.995, 9), ((300, 200, 64), 0.999, 10), ((130, 140, 70), 0.98, 11),
     ((257, 129, 33), 0.7, 12),
+    # widths that are multiples of 16 take the 16-voxels-per-lane x pass: an odd
+    # number of 16-voxel groups (48), a single group (16), more than 32 groups (528)
+    ((5, 9, 48), 0.6, 13), ((3, 4, 16), 0.5, 14), ((6, 10, 528), 0.9, 15),
 ]
 
 
@@ -178,6 +181,18 @@ def test_tbth_tbsp_small_random_specimens(gpu_ctx, seed):
     shape = tuple(int(v) for v in rng.integers(20, 70, size=3))
     sp = S.make_specimen(shape, float(rng.uniform(1.5, 3)), float(rng.uniform(0.1, 0.4)), "cylinder",
                          0.45 * min(shape[1], shape[2]), float(rng.uniform(5, 25)), seed)
+    res = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx, return_maps=True)
+    for sel, got, gmap in ((True, res.thickness, res.thickness_map), (False, res.spacing, res.spacing_map)):
+        m = O.phase_inside(sp.bone, sp.roi, sel)
+        ref = O.local_thickness(m, O.FOREGROUND)
+        assert np.array_equal(gmap.view(np.uint32), ref.thickness.view(np.uint32))
+        check_stats(got, ref.thickness, sp.spacing_um)
+
+
+@pytest.mark.parametrize("shape", [(20, 24, 48), (9, 12, 528), (11, 13, 47)])
+def test_tbth_tbsp_row_widths(gpu_ctx, shape):
+    """Tb.Th / Tb.Sp maps bit-exact for widths on and off the 16-voxel x-pass path."""
+    sp = S.make_specimen(shape, 2.0, 0.3, "cylinder", 0.45 * min(shape[1], shape[2]), 12.0, 31)
     res = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx, return_maps=True)
     for sel, got, gmap in ((True, res.thickness, res.thickness_map), (False, res.spacing, res.spacing_map)):
         m = O.phase_inside(sp.bone, sp.roi, sel)
