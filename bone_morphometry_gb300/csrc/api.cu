@@ -315,14 +315,29 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   fill_phase(ctx, dm, ridges, ctr, res.selected, hc.rmax, occ, selbits, F, s);
   StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));
   check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
+  FixedPartial* part = static_cast<FixedPartial*>(
+      ensure(ctx, ctx->cpart, kCleanupMaxGrid * sizeof(FixedPartial), "stats partials"));
+  // every value of the map is at least 2 * scale (diameters are >= 2), so its
+  // f32 exponent is at least that of 2 * scale: the fixed-point base
+  const float two_s = 2.0f * scale;
+  uint32_t tb;
+  std::memcpy(&tb, &two_s, 4);
+  const int e2s = (int)(tb >> 23);
+  const int e_lo = (e2s >= 1 && e2s + kFixedSpan <= 254) ? e2s : 4096;  // 4096: no fixed-point path
+  unsigned cgrid = 0;
   timed(ctx, KF_CLEAN_FINAL, s, "cleanup",
         [&] {
-          return launch_cleanup(F, selbits, dm, static_cast<const float*>(ctx->lutf.ptr), scale, d_map, acc, s,
-                                &ctx->launches);
+          return launch_cleanup(F, selbits, dm, static_cast<const float*>(ctx->lutf.ptr), scale, d_map, acc, part,
+                                e_lo, &cgrid, s, &ctx->launches);
         });
+  std::vector<FixedPartial> hpart(cgrid);
   check(ctx, cudaMemcpyAsync(&res.acc, acc, sizeof(StatsAccum), cudaMemcpyDeviceToHost, s), "stats readback");
+  if (cgrid)
+    check(ctx, cudaMemcpyAsync(hpart.data(), part, cgrid * sizeof(FixedPartial), cudaMemcpyDeviceToHost, s),
+          "stats readback");
   check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
   check(ctx, cudaStreamSynchronize(s), "local thickness");
+  if (e_lo != 4096) fold_fixed_partials(res.acc, hpart.data(), cgrid, e_lo);
   res.ridges = hc.ridges;
 }
 
@@ -619,7 +634,7 @@ void set_thread_error(const char* msg) { g_create_error = msg; }
 
 size_t cached_bytes(const bm_ctx* ctx) {
   const Buffer* all[] = {&ctx->in_a,     &ctx->in_b,       &ctx->dist,       &ctx->dist2,       &ctx->stack,
-                         &ctx->fillmap,  &ctx->selbits,    &ctx->posbits,    &ctx->ridges,      &ctx->accum,
+                         &ctx->fillmap,  &ctx->selbits,    &ctx->posbits,    &ctx->ridges,      &ctx->accum,      &ctx->cpart,
                          &ctx->outmap,   &ctx->outmap2,    &ctx->occ,        &ctx->rank,        &ctx->rvals,
                          &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
                          &ctx->qhist,    &ctx->qtargets,   &ctx->qmap,       &ctx->rgeo};
@@ -665,7 +680,7 @@ int bm_ctx_trim(bm_ctx* ctx) {
   return guarded(ctx, [&]() -> int {
     cudaStreamSynchronize(ctx->stream);
     Buffer* all[] = {&ctx->in_a,  &ctx->in_b,      &ctx->dist,       &ctx->dist2,      &ctx->stack,
-                     &ctx->fillmap, &ctx->selbits,  &ctx->posbits,   &ctx->ridges,     &ctx->accum,
+                     &ctx->fillmap, &ctx->selbits,  &ctx->posbits,   &ctx->ridges,     &ctx->accum,      &ctx->cpart,
                      &ctx->outmap, &ctx->outmap2,  &ctx->occ,       &ctx->rank,       &ctx->rvals,
                      &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
                      &ctx->qhist, &ctx->qtargets, &ctx->qmap, &ctx->rgeo};
@@ -687,7 +702,7 @@ void bm_ctx_destroy(bm_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     Buffer* all[] = {&ctx->lut,      &ctx->in_a,      &ctx->in_b,       &ctx->dist,     &ctx->dist2,
                      &ctx->stack,    &ctx->fillmap,   &ctx->selbits,    &ctx->posbits,  &ctx->ridges,
-                     &ctx->counters, &ctx->accum,     &ctx->outmap,     &ctx->outmap2,  &ctx->host_pinned,
+                     &ctx->counters, &ctx->accum,     &ctx->cpart,     &ctx->outmap,     &ctx->outmap2,  &ctx->host_pinned,
                      &ctx->occ,      &ctx->rank,      &ctx->rvals,      &ctx->fillinfo, &ctx->bincounts,
                      &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
                      &ctx->qhist,    &ctx->qtargets,  &ctx->qmap,     &ctx->rgeo};

@@ -39,6 +39,25 @@ struct StatsAccum {
   unsigned long long count;
   unsigned int max_bits;
   unsigned int pad;
+  // Fixed-point totals (filled on the host from FixedPartial records):
+  // sum of m * 2^(e - e_lo) and of m^2 * 2^(2 (e - e_lo)) over the values
+  // whose exponent e lies in [e_lo, e_lo + kFixedSpan]; fx_elo = 0: none.
+  unsigned long long fx_s1[2];
+  unsigned long long fx_s2[3];
+  int fx_elo;
+  int fx_pad;
+};
+
+// Exponent span of the fixed-point statistics path (values of one map lie
+// within 2^16 of their smallest possible value).
+constexpr int kFixedSpan = 20;
+
+// One CTA's fixed-point statistics: s1 (sum of shifted mantissas) and the
+// 128-bit sum of their squares.
+struct FixedPartial {
+  unsigned long long s1;
+  unsigned long long s2lo, s2hi;
+  unsigned long long pad;
 };
 
 // Tile of the tile-owned sphere fill (x, y, z voxels).
@@ -119,6 +138,7 @@ struct bm_ctx {
   bm::Buffer ridges;           // ridge records
   bm::Buffer counters;         // bm::Counters
   bm::Buffer accum;            // bm::StatsAccum
+  bm::Buffer cpart;            // bm::FixedPartial per cleanup CTA
   bm::Buffer outmap;           // f32 output staging
   bm::Buffer outmap2;
   bm::Buffer host_pinned;      // pinned staging for small readbacks

@@ -2,6 +2,8 @@
 //
 // The device accumulates, per f32 exponent e (value = m * 2^(e-150) with a
 // 24-bit integer m), the integer sums of m and of m*m (split as hi*2^24 + lo).
+// Values whose exponent lies within kFixedSpan of a known smallest exponent
+// e_lo arrive instead as per-CTA sums of m * 2^(e - e_lo) and their squares.
 // Here those integers are placed into a wide fixed-point integer and the total
 // is rounded to the nearest f64 (ties to even).  The result is the correctly
 // rounded exact sum, independent of the order in which the GPU added values.
@@ -81,6 +83,29 @@ struct WideUInt {
   }
 };
 
+// Adds the per-CTA fixed-point partials into a's host-side totals.
+inline void fold_fixed_partials(StatsAccum& a, const FixedPartial* p, unsigned n, int e_lo) {
+  unsigned long long s1[2] = {a.fx_s1[0], a.fx_s1[1]};
+  unsigned long long s2[3] = {a.fx_s2[0], a.fx_s2[1], a.fx_s2[2]};
+  for (unsigned i = 0; i < n; ++i) {
+    s1[0] += p[i].s1;
+    s1[1] += (s1[0] < p[i].s1) ? 1u : 0u;
+    const unsigned long long lo = s2[0] + p[i].s2lo;
+    const unsigned long long c0 = lo < s2[0] ? 1u : 0u;
+    s2[0] = lo;
+    const unsigned long long mid = s2[1] + p[i].s2hi;
+    const unsigned long long c1 = mid < s2[1] ? 1u : 0u;
+    s2[1] = mid + c0;
+    s2[2] += c1 + ((s2[1] < c0) ? 1u : 0u);
+  }
+  a.fx_s1[0] = s1[0];
+  a.fx_s1[1] = s1[1];
+  a.fx_s2[0] = s2[0];
+  a.fx_s2[1] = s2[1];
+  a.fx_s2[2] = s2[2];
+  a.fx_elo = e_lo;
+}
+
 inline void exact_sums_to_double(const StatsAccum& a, double* sum, double* sum_sq) {
   WideUInt s, q;
   for (int e = 1; e < 256; ++e) {
@@ -89,6 +114,15 @@ inline void exact_sums_to_double(const StatsAccum& a, double* sum, double* sum_s
     // squares: m^2 * 2^(2e-300), LSB 2^-298 -> shift 2e-2
     q.add_shifted(a.sq_lo[e], 2 * e - 2);
     q.add_shifted(a.sq_hi[e], 2 * e - 2 + 24);
+  }
+  if (a.fx_elo > 0) {
+    // fixed point: units of 2^(e_lo - 150) for the sum, 2^(2 e_lo - 300) for squares
+    const int e = a.fx_elo;
+    s.add_shifted(a.fx_s1[0], e - 1);
+    s.add_shifted(a.fx_s1[1], e - 1 + 64);
+    q.add_shifted(a.fx_s2[0], 2 * e - 2);
+    q.add_shifted(a.fx_s2[1], 2 * e - 2 + 64);
+    q.add_shifted(a.fx_s2[2], 2 * e - 2 + 128);
   }
   *sum = s.to_double(149);
   *sum_sq = q.to_double(298);

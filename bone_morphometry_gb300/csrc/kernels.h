@@ -53,8 +53,13 @@ cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long 
 
 // Fused cleanup passes 1 and 2, phase mask, optional f32 map, exact statistics.
 // dia: f32 diameters 2*sqrt(r2) by r2 (launch_dia_table).
+// Values whose f32 exponent lies in [e_lo, e_lo + kFixedSpan] are summed in
+// fixed point, one FixedPartial per CTA in part[0 .. *grid); the others go to
+// acc's per-exponent sums.  At most kCleanupMaxGrid CTAs.
+constexpr unsigned kCleanupMaxGrid = 4096;
 cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const float* dia, float scale,
-                           float* outmap, StatsAccum* acc, cudaStream_t s, unsigned long long* launches);
+                           float* outmap, StatsAccum* acc, FixedPartial* part, int e_lo, unsigned* grid,
+                           cudaStream_t s, unsigned long long* launches);
 cudaError_t launch_dia_table(const uint4* lut, uint32_t n, float* dia, cudaStream_t s, unsigned long long* launches);
 
 // Tile-owned fill (fill.cu).

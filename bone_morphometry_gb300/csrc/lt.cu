@@ -134,9 +134,12 @@ __device__ __forceinline__ void flush_run(StatsAccum& sacc, uint32_t e, unsigned
   }
 }
 
-// One value of the calibrated map into this thread's statistics.
-__device__ __forceinline__ void add_value(float val, float scale, unsigned long long& cnt, uint32_t& mx,
-                                          uint32_t& run_e, unsigned long long& run_s1, unsigned long long& run_sh,
+// One value of the calibrated map into this thread's statistics: in fixed
+// point when its exponent is within kFixedSpan of e_lo (no atomics), else into
+// the per-exponent run.
+__device__ __forceinline__ void add_value(float val, float scale, int e_lo, unsigned long long& cnt, uint32_t& mx,
+                                          unsigned long long& fx1, unsigned __int128& fx2, uint32_t& run_e,
+                                          unsigned long long& run_s1, unsigned long long& run_sh,
                                           unsigned long long& run_sl, StatsAccum& sacc) {
   const uint32_t bits = __float_as_uint(__fmul_rn(val, scale));
   ++cnt;
@@ -144,6 +147,13 @@ __device__ __forceinline__ void add_value(float val, float scale, unsigned long 
   uint32_t e = bits >> 23, m = bits & 0x7fffffu;
   if (e) m |= 0x800000u;
   else e = 1;
+  const uint32_t sh = e - (uint32_t)e_lo;
+  if (sh <= (uint32_t)kFixedSpan) {
+    const unsigned long long m64 = m;
+    fx1 += m64 << sh;
+    fx2 += (unsigned __int128)(m64 * m64) << (2 * sh);
+    return;
+  }
   if (e != run_e) {  // a new exponent: flush this thread's run
     flush_run(sacc, run_e, run_s1, run_sh, run_sl);
     run_e = e;
@@ -157,7 +167,8 @@ __device__ __forceinline__ void add_value(float val, float scale, unsigned long 
 __global__ void __launch_bounds__(kCleanThreads)
 cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict__ selbits, Dims dm,
                     const float* __restrict__ dia, float scale, float* __restrict__ outmap,
-                    StatsAccum* __restrict__ acc, int ntx, int nty, int ntz) {
+                    StatsAccum* __restrict__ acc, FixedPartial* __restrict__ part, int e_lo, int ntx, int nty,
+                    int ntz) {
   __shared__ uint32_t T[kCSZ * kCSY * kCSX];         // f32 diameter bits of the r^2 map
   __shared__ unsigned long long nz[kCSZ * kCSY];     // bit x: T != 0 (or out of volume)
   __shared__ unsigned long long inr[kCSZ * kCSY];    // bit x: interior (pass-1 value kept)
@@ -181,6 +192,9 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
   // changes, so a thread's values are added once, without warp votes)
   uint32_t run_e = 0;
   unsigned long long run_s1 = 0, run_sh = 0, run_sl = 0;
+  // fixed-point sums of the values with exponent in [e_lo, e_lo + kFixedSpan]
+  unsigned long long fx1 = 0;
+  unsigned __int128 fx2 = 0;
   const long long ntiles = (long long)ntx * nty * ntz;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
@@ -284,13 +298,40 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
         }
       }
       if (orow && x < dm.w) orow[x] = val;
-      if (val > 0.0f) add_value(val, scale, cnt, mx, run_e, run_s1, run_sh, run_sl, sacc);
+      if (val > 0.0f) add_value(val, scale, e_lo, cnt, mx, fx1, fx2, run_e, run_s1, run_sh, run_sl, sacc);
     }
   }
   flush_run(sacc, run_e, run_s1, run_sh, run_sl);
   if (cnt) atomicAdd(&sacc.count, cnt);
   if (mx) atomicMax(&sacc.max_bits, mx);
+  // this CTA's fixed-point sums: warp reduction, then one record per CTA
+  unsigned long long f2lo = (unsigned long long)fx2, f2hi = (unsigned long long)(fx2 >> 64);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    fx1 += __shfl_xor_sync(0xffffffffu, fx1, o);
+    const unsigned long long olo = __shfl_xor_sync(0xffffffffu, f2lo, o);
+    const unsigned long long ohi = __shfl_xor_sync(0xffffffffu, f2hi, o);
+    const unsigned long long lo = f2lo + olo;
+    f2hi += ohi + (lo < f2lo ? 1u : 0u);
+    f2lo = lo;
+  }
+  __shared__ unsigned long long s_fx[kCleanThreads / 32][3];
+  if (lane == 0) {
+    s_fx[warp][0] = fx1;
+    s_fx[warp][1] = f2lo;
+    s_fx[warp][2] = f2hi;
+  }
   __syncthreads();
+  if (tid == 0) {
+    FixedPartial r{0ull, 0ull, 0ull, 0ull};
+    for (int w = 0; w < kCleanThreads / 32; ++w) {
+      r.s1 += s_fx[w][0];
+      const unsigned long long lo = r.s2lo + s_fx[w][1];
+      r.s2hi += s_fx[w][2] + (lo < r.s2lo ? 1u : 0u);
+      r.s2lo = lo;
+    }
+    part[blockIdx.x] = r;
+  }
   for (int i = tid; i < 256; i += kCleanThreads) {
     if (sacc.sum_m[i]) atomicAdd(&acc->sum_m[i], sacc.sum_m[i]);
     if (sacc.sq_hi[i]) atomicAdd(&acc->sq_hi[i], sacc.sq_hi[i]);
@@ -458,11 +499,15 @@ cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long 
 }
 
 cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const float* dia, float scale,
-                           float* outmap, StatsAccum* acc, cudaStream_t s, unsigned long long* launches) {
+                           float* outmap, StatsAccum* acc, FixedPartial* part, int e_lo, unsigned* grid,
+                           cudaStream_t s, unsigned long long* launches) {
   const int ntx = (dm.w + kCTX - 1) / kCTX, nty = (dm.h + kCTY - 1) / kCTY, ntz = (dm.d + kCTZ - 1) / kCTZ;
   const long long tiles = (long long)ntx * nty * ntz;
-  const unsigned grid = resident_grid(cleanup_tile_kernel, kCleanThreads, 0, tiles);
-  cleanup_tile_kernel<<<grid, kCleanThreads, 0, s>>>(fillmap, selbits, dm, dia, scale, outmap, acc, ntx, nty, ntz);
+  unsigned g = resident_grid(cleanup_tile_kernel, kCleanThreads, 0, tiles);
+  if (g > kCleanupMaxGrid) g = kCleanupMaxGrid;
+  *grid = g;
+  cleanup_tile_kernel<<<g, kCleanThreads, 0, s>>>(fillmap, selbits, dm, dia, scale, outmap, acc, part, e_lo, ntx, nty,
+                                                  ntz);
   ++*launches;
   return cudaGetLastError();
 }
