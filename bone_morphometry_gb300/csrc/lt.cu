@@ -164,7 +164,7 @@ __device__ __forceinline__ void add_value(float val, float scale, int e_lo, unsi
   run_sl += sq & 0xffffffu;
 }
 
-__global__ void __launch_bounds__(kCleanThreads)
+__global__ void __launch_bounds__(kCleanThreads, 3)
 cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict__ selbits, Dims dm,
                     const float* __restrict__ dia, float scale, float* __restrict__ outmap,
                     StatsAccum* __restrict__ acc, FixedPartial* __restrict__ part, int e_lo, int ntx, int nty,
@@ -223,9 +223,17 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
       for (int j = 0; j < kBatch; ++j) {
         const int r = warp + (kCleanThreads / 32) * (b + j);
         uint32_t* srow = T + r * kCSX;
-        // staged as the f32 diameter bits (2*sqrt(r^2)); 0 stays 0
-        srow[lane] = (v[j] == 0u || v[j] == kOob) ? 0u : __float_as_uint(dia[v[j]]);
-        if (lane < kCSX - 32) srow[32 + lane] = (v2[j] == 0u || v2[j] == kOob) ? 0u : __float_as_uint(dia[v2[j]]);
+        // staged as the f32 diameter bits (2*sqrt(r^2)), 0 staying 0; pass 2
+        // reads diameters only within one voxel of the tile, so the outer
+        // ring keeps just its nonzero flags
+        const int rz = r / kCSY, ry = r % kCSY;
+        const bool ring = rz == 0 || rz == kCSZ - 1 || ry == 0 || ry == kCSY - 1;
+        if (!ring) {
+          srow[lane] = (lane == 0 || v[j] == 0u || v[j] == kOob) ? 0u : __float_as_uint(dia[v[j]]);
+          if (lane < kCSX - 32)
+            srow[32 + lane] =
+                (lane == kCSX - 33 || v2[j] == 0u || v2[j] == kOob) ? 0u : __float_as_uint(dia[v2[j]]);
+        }
         const unsigned b1 = __ballot_sync(0xffffffffu, v[j] != 0u);
         const unsigned b2 = __ballot_sync(0xffffffffu, lane < kCSX - 32 && v2[j] != 0u);
         const unsigned o1 = __ballot_sync(0xffffffffu, v[j] != 0u && v[j] != kOob);

@@ -110,3 +110,18 @@ def test_volume_metrics_random(gpu_ctx):
         for sh in (-1, 1):
             nb |= ~np.roll(rp, sh, axis=ax)[1:-1, 1:-1, 1:-1]
     assert vm.boundary_bone_voxels == int((b & nb).sum())
+
+
+@pytest.mark.parametrize("spacing", [1e-39, 3e-38, 0.37, 7.5e33])
+def test_tbth_tbsp_exact_sums_at_extreme_spacings(gpu_ctx, spacing):
+    """Fixed-point and per-exponent statistic paths (subnormal, tiny, ordinary
+    and huge calibrations) against an exact summation of the oracle's maps."""
+    sp = S.make_specimen((24, 26, 28), 2.0, 0.3, "cylinder", 11.0, spacing, 41)
+    res = analyze_thickness(sp.bone, sp.roi, spacing, ctx=gpu_ctx)
+    for sel, got in ((True, res.thickness), (False, res.spacing)):
+        ref = O.local_thickness(O.phase_inside(sp.bone, sp.roi, sel), O.FOREGROUND).thickness
+        n, s, ss, mx = O.exact_moment_sums(ref, spacing)
+        mean, sd, mxr = O.stats_from_sums(n, s, ss, mx)
+        assert got.count == n
+        assert got.sum == s and got.sum_of_squares == ss
+        assert got.mean == mean and got.standard_deviation == sd and got.maximum == mxr
