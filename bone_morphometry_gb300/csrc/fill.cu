@@ -206,10 +206,11 @@ __device__ __forceinline__ uint32_t sel_word(const uint32_t* __restrict__ selbit
 }
 
 constexpr int kBinChunk = 256;    // bins whose offsets are staged in shared memory at a time
-constexpr int kEntWin = 1024;     // ball entries staged in shared memory at a time
+constexpr int kEntWin = 768;      // ball entries staged in shared memory at a time
 constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself)
 constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
 constexpr int kItems = 1024;      // (ball, plane) paint items per round
+constexpr int kHxMax = 31;        // balls up to this radius read their chord half-widths from a table
 constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
 
 // rot[lv - 1][z][y] = OR of the unpainted-voxel masks of rows y .. y + 2^lv - 1
@@ -236,7 +237,8 @@ __device__ __forceinline__ int vidx(int row, int x) {
 }
 
 constexpr size_t kTileFillSmemWords =
-    (size_t)kRows * 16 + kRows + (kBinChunk + 4) + kBinChunk + kEntWin + (kRotLevels - 1) * kFillTZ * 32 + kItems;
+    (size_t)kRows * 16 + kRows + (kBinChunk + 4) + kBinChunk + kEntWin + (kRotLevels - 1) * kFillTZ * 32 + kItems +
+    130 + (kHxMax + 1) * (kHxMax + 1) / 4;
 
 // One CTA per tile (32 x 32 x 16 voxels) paints the tile's selected voxels.
 // Shared memory:
@@ -273,6 +275,8 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
   uint32_t* ent = nzb + kBinChunk;                           // kEntWin
   uint32_t* rot = ent + kEntWin;                             // (kRotLevels - 1) * kFillTZ * 32
   uint32_t* item = rot + (kRotLevels - 1) * kFillTZ * 32;    // kItems
+  uint16_t* hyt = reinterpret_cast<uint16_t*>(item + kItems);              // 257 (+1) half-words
+  uint8_t* hxt = reinterpret_cast<uint8_t*>(item + kItems + 130);         // (kHxMax + 1)^2 bytes
   __shared__ uint32_t s_nnz, s_wlo, s_whi;
   __shared__ uint32_t s_nitem[2];
   __shared__ uint32_t wcnt[kFillWarps];
@@ -347,6 +351,18 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
         const uint16_t tag = (uint16_t)(b0 + bl + 1u);
         const int rad = (int)gq.z;                         // isqrt(r2): no lattice point of the ball is further
         const uint32_t e = boff[bl + 1];
+        // this bin's disk radii: hyt[|dz|] = isqrt(r2 - dz^2); for small balls
+        // also the chord half-widths hxt[|dz| * 32 + |dy|] = isqrt(r2 - dz^2 - dy^2)
+        for (int i = tid; i <= rad; i += kFillThreads) hyt[i] = (uint16_t)isqrt24((uint32_t)(R - i * i));
+        if (rad <= kHxMax) {
+          for (int i = tid; i < (rad + 1) * 32; i += kFillThreads) {
+            const int a = i >> 5, c = i & 31;
+            const int t = R - a * a - c * c;
+            hxt[i] = t >= 0 ? (uint8_t)isqrt24((uint32_t)t) : (uint8_t)0;
+          }
+        }
+        if (k % kRotEvery == 0 && k > 0) build_rot(usel, rot, warp, lane, kFillWarps);
+        __syncthreads();
         for (uint32_t ss = boff[bl]; ss < e;) {
           if (ss < s_wlo || ss >= s_whi) {  // reload the entry window at ss (uniform decision)
             __syncthreads();
@@ -379,7 +395,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
               const int dz = zz - cz;
               const int prem = R - dz * dz;
               if (prem >= 0) {
-                const int hy = (int)isqrt24((uint32_t)prem);
+                const int hy = (int)hyt[abs(dz)];
                 pya = max(cy - hy, 0);
                 pyb = min(cy + hy, vy - 1);
                 const int xa = max(cx - hy, 0), xb = min(cx + hy, vx - 1);
@@ -430,7 +446,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             const int row = zz * kFillTY + y;
             const uint32_t m = usel[row];
             if (!m) return;
-            const int hx = (int)isqrt24((uint32_t)t);
+            const int hx = rad <= kHxMax ? (int)hxt[abs(dz) * 32 + abs(dy)] : (int)isqrt24((uint32_t)t);
             const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
             if (xa > xb) return;
             uint32_t bits = m & range_mask(xa, xb);
@@ -448,10 +464,6 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
           parity ^= 1u;
           __syncthreads();
           ss = se;
-        }
-        if (k % kRotEvery == kRotEvery - 1) {
-          build_rot(usel, rot, warp, lane, kFillWarps);
-          __syncthreads();
         }
       }
     }
