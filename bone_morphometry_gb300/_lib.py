@@ -82,7 +82,8 @@ class BmSpecimen(ctypes.Structure):
 
 class BmResult(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("thickness", BmStats), ("spacing", BmStats), ("submit_s", ctypes.c_double),
-                ("start_s", ctypes.c_double), ("end_s", ctypes.c_double), ("footprint_bytes", ctypes.c_uint64)]
+                ("start_s", ctypes.c_double), ("end_s", ctypes.c_double), ("footprint_bytes", ctypes.c_uint64),
+                ("message", ctypes.c_char * 256)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/bm.h
@@ -122,11 +123,15 @@ SIGNATURES = {
     "bm_ctx_set_workers": (_i, [_pctx, _i]),
     "bm_server_create": (_i, [_i, _i, _d, ctypes.POINTER(ctypes.c_void_p)]),
     "bm_server_submit": (_i, [_vp, ctypes.POINTER(BmSpecimen), _u, ctypes.POINTER(ctypes.c_uint64)]),
+    "bm_server_submit_tiff": (_i, [_vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, _i, _d, _u,
+                                   ctypes.POINTER(ctypes.c_uint64)]),
     "bm_server_poll": (_i, [_vp, ctypes.c_uint64, _i, ctypes.POINTER(BmResult)]),
     "bm_server_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                              ctypes.POINTER(ctypes.c_double)]),
     "bm_server_destroy": (None, [_vp]),
     "bm_footprint_bytes": (ctypes.c_uint64, [_sz, _sz, _sz]),
+    "bm_tiff_read": (_i, [ctypes.c_char_p, ctypes.c_uint, _i, _vp, _sz, ctypes.POINTER(_sz), ctypes.POINTER(_sz),
+                          ctypes.POINTER(_sz)]),
 }
 
 _LIB = None

@@ -10,10 +10,12 @@
 // specimen's results do not depend on what else is in flight.
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -33,11 +35,41 @@ struct Job {
   bm_specimen sp{};
   unsigned flags = 0;
   bool device = false;
+  // TIFF-path request: stacks decoded on the worker (bone_path not empty)
+  std::string bone_path, roi_path;
+  unsigned threshold = 0;
+  bool strict = false;
   uint64_t id = 0;
   uint64_t bytes = 0;
   bm_result res{};
   bool done = false;
 };
+
+// A worker's page-locked staging for TIFF-path requests (grown on demand).
+struct PinnedStage {
+  uint8_t* p = nullptr;
+  size_t n = 0;
+  ~PinnedStage() {
+    if (p) cudaFreeHost(p);
+  }
+  uint8_t* get(size_t bytes) {
+    if (bytes <= n) return p;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    if (cudaHostAlloc(reinterpret_cast<void**>(&p), bytes, cudaHostAllocDefault) != cudaSuccess) {
+      p = nullptr;
+      return nullptr;
+    }
+    n = bytes;
+    return p;
+  }
+};
+
+void copy_message(bm_result& r, const char* msg) {
+  std::strncpy(r.message, msg ? msg : "", sizeof r.message - 1);
+  r.message[sizeof r.message - 1] = 0;
+}
 
 }  // namespace
 
@@ -99,6 +131,7 @@ class Pool {
  private:
   void worker_main(int w) {
     bm_ctx* ctx = ctxs_[w];
+    PinnedStage bone_stage, roi_stage;
     for (;;) {
       Job* j = nullptr;
       {
@@ -113,7 +146,7 @@ class Pool {
         ++running_;
         j->res.start_s = now_s();
       }
-      run(ctx, j);
+      run(ctx, j, bone_stage, roi_stage);
       const double job_bytes = (double)j->bytes;
       {
         std::lock_guard<std::mutex> lk(mu_);
@@ -134,7 +167,12 @@ class Pool {
     }
   }
 
-  static void run(bm_ctx* ctx, Job* j) {
+  static void run(bm_ctx* ctx, Job* j, PinnedStage& bone_stage, PinnedStage& roi_stage) {
+    j->res.footprint_bytes = j->bytes;
+    if (!j->bone_path.empty()) {
+      run_tiff(ctx, j, bone_stage, roi_stage);
+      return;
+    }
     const bm_specimen& s = j->sp;
     if (j->device)
       j->res.status = bm_tbth_tbsp_device(ctx, s.bone, s.roi, s.width, s.height, s.depth, s.spacing_um, j->flags,
@@ -142,7 +180,65 @@ class Pool {
     else
       j->res.status = bm_tbth_tbsp(ctx, s.bone, s.roi, s.width, s.height, s.depth, s.spacing_um, j->flags,
                                    &j->res.thickness, &j->res.spacing, nullptr, nullptr);
-    j->res.footprint_bytes = j->bytes;
+    if (j->res.status != BM_OK) {
+      char buf[256];
+      bm_last_error(ctx, buf, sizeof buf);
+      copy_message(j->res, buf);
+    }
+  }
+
+  // Decode the stacks into this worker's page-locked buffers, then run the
+  // specimen from there (tiff_io.rs:19-31 for the stacks, main.rs for the ROI
+  // default: every voxel).
+  static void run_tiff(bm_ctx* ctx, Job* j, PinnedStage& bone_stage, PinnedStage& roi_stage) {
+    char buf[256];
+    size_t w = 0, h = 0, d = 0;
+    int st = bm_tiff_read(j->bone_path.c_str(), j->threshold, j->strict ? BM_TIFF_ZERO_OR_255 : BM_TIFF_ANY, nullptr,
+                          0, &w, &h, &d);
+    const size_t n = w * h * d;
+    uint8_t* bone = nullptr;
+    uint8_t* roi = nullptr;
+    if (st == BM_OK) {
+      bone = bone_stage.get(n);
+      roi = roi_stage.get(n);
+      if (!bone || !roi) {
+        j->res.status = BM_ERR_OOM;
+        copy_message(j->res, "page-locked staging allocation failed");
+        return;
+      }
+      st = bm_tiff_read(j->bone_path.c_str(), j->threshold, j->strict ? BM_TIFF_ZERO_OR_255 : BM_TIFF_ANY, bone, n,
+                        &w, &h, &d);
+    }
+    if (st == BM_OK) {
+      if (j->roi_path.empty()) {
+        std::memset(roi, 1, n);
+      } else {
+        size_t rw = 0, rh = 0, rd = 0;
+        st = bm_tiff_read(j->roi_path.c_str(), 0, BM_TIFF_ROI_MASK, nullptr, 0, &rw, &rh, &rd);
+        if (st == BM_OK && rw == w && rh == h && rd == d)
+          st = bm_tiff_read(j->roi_path.c_str(), 0, BM_TIFF_ROI_MASK, roi, n, &rw, &rh, &rd);
+        if (st == BM_OK && (rw != w || rh != h || rd != d)) {
+          // metrics.rs:79-89
+          std::snprintf(buf, sizeof buf, "binary image dimensions %zux%zux%zu do not match ROI dimensions %zux%zux%zu",
+                        w, h, d, rw, rh, rd);
+          j->res.status = BM_ERR_INVALID;
+          copy_message(j->res, buf);
+          return;
+        }
+      }
+    }
+    if (st != BM_OK) {
+      bm_last_error(nullptr, buf, sizeof buf);
+      j->res.status = st;
+      copy_message(j->res, buf);
+      return;
+    }
+    j->res.status = bm_tbth_tbsp(ctx, bone, roi, w, h, d, j->sp.spacing_um, j->flags, &j->res.thickness,
+                                 &j->res.spacing, nullptr, nullptr);
+    if (j->res.status != BM_OK) {
+      bm_last_error(ctx, buf, sizeof buf);
+      copy_message(j->res, buf);
+    }
   }
 
   int device_;
@@ -250,6 +346,35 @@ int bm_server_submit(bm_server* srv, const bm_specimen* item, unsigned flags, ui
   j->flags = flags;
   j->device = false;
   j->bytes = bm_footprint_bytes(item->width, item->height, item->depth);
+  if ((double)j->bytes > srv->pool->budget()) return BM_ERR_BUSY;
+  Job* raw = j.get();
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    j->id = srv->next++;
+    *ticket = j->id;
+    srv->jobs.emplace(j->id, std::move(j));
+  }
+  srv->pool->submit(raw);
+  return BM_OK;
+}
+
+int bm_server_submit_tiff(bm_server* srv, const char* bone_path, const char* roi_path, unsigned threshold,
+                          int strict_binary, double spacing_um, unsigned flags, uint64_t* ticket) {
+  if (!srv || !bone_path || !ticket || threshold > 255) return BM_ERR_INVALID;
+  size_t w = 0, h = 0, d = 0;
+  const int st = bm_tiff_read(bone_path, threshold, BM_TIFF_ANY, nullptr, 0, &w, &h, &d);  // headers only
+  if (st != BM_OK) return st;
+  auto j = std::make_unique<Job>();
+  j->bone_path = bone_path;
+  if (roi_path) j->roi_path = roi_path;
+  j->threshold = threshold;
+  j->strict = strict_binary != 0;
+  j->sp.width = w;
+  j->sp.height = h;
+  j->sp.depth = d;
+  j->sp.spacing_um = spacing_um;
+  j->flags = flags;
+  j->bytes = bm_footprint_bytes(w, h, d);
   if ((double)j->bytes > srv->pool->budget()) return BM_ERR_BUSY;
   Job* raw = j.get();
   {

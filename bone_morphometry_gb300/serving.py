@@ -13,6 +13,7 @@ per-specimen arithmetic, so every result equals the specimen's result alone.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -81,6 +82,7 @@ class Result:
     start_s: float
     end_s: float
     footprint_bytes: int
+    message: str = ""  # error text when status != 0
 
     @property
     def latency_s(self) -> float:
@@ -109,6 +111,19 @@ class Server:
         self._inputs[t.value] = sp  # keep the host buffers alive until the result is taken
         return t.value
 
+    def submit_tiff(self, bone_path, roi_path=None, spacing_um: float = 1.0, threshold: int = 0,
+                    strict_binary: bool = False, feature_mode=FeatureMode.CLASSIC) -> int:
+        """A request read from TIFF stacks on the worker (tiff_io.rs:19-31): decoded
+        into the worker's page-locked buffers, no host copy in between."""
+        t = ctypes.c_uint64()
+        st = self._lib.bm_server_submit_tiff(self.handle, os.fsencode(os.fspath(bone_path)),
+                                             None if roi_path is None else os.fsencode(os.fspath(roi_path)),
+                                             int(threshold), 1 if strict_binary else 0, float(spacing_um),
+                                             _flags(feature_mode), ctypes.byref(t))
+        if st != BM_OK:
+            raise BoneMorphometryError(st, "request exceeds the HBM budget" if st == BM_ERR_BUSY else last_error(None))
+        return t.value
+
     def result(self, ticket: int, wait: bool = True):
         r = BmResult()
         st = self._lib.bm_server_poll(self.handle, ctypes.c_uint64(ticket), 1 if wait else 0, ctypes.byref(r))
@@ -118,7 +133,7 @@ class Server:
             raise BoneMorphometryError(st, "unknown ticket %d" % ticket)
         self._inputs.pop(ticket, None)
         return Result(ticket, r.status, DistributionStats.from_c(r.thickness), DistributionStats.from_c(r.spacing),
-                      r.submit_s, r.start_s, r.end_s, int(r.footprint_bytes))
+                      r.submit_s, r.start_s, r.end_s, int(r.footprint_bytes), r.message.decode("utf-8", "replace"))
 
     def stats(self):
         q, run, b = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()

@@ -220,10 +220,20 @@ typedef struct bm_result {
   bm_stats spacing;
   double submit_s, start_s, end_s; /* seconds on a steady clock */
   uint64_t footprint_bytes;
+  char message[256];               /* error text when status != BM_OK */
 } bm_result;
 int bm_server_create(int device, int workers, double hbm_budget_bytes, bm_server** out);
 /* BM_ERR_BUSY if the request alone exceeds the budget. */
 int bm_server_submit(bm_server* srv, const bm_specimen* item, unsigned flags, uint64_t* ticket);
+/* A request read from TIFF stacks on the worker (bm_tiff_read semantics): the
+ * bone stack (threshold, strict 0/255 check when strict_binary != 0) and the
+ * ROI stack (0/1/255; roi_path NULL = every voxel in the ROI, as the reference
+ * does without an ROI directory) are decoded straight into the worker's
+ * page-locked buffers and copied to the GPU from there.  The stacks' headers
+ * are read at submission to size the request; decoding errors come back in
+ * the result (status and message). */
+int bm_server_submit_tiff(bm_server* srv, const char* bone_path, const char* roi_path, unsigned threshold,
+                          int strict_binary, double spacing_um, unsigned flags, uint64_t* ticket);
 /* wait != 0: block until the ticket completes; else BM_ERR_BUSY while pending.
  * A completed ticket's result is returned once and then forgotten. */
 int bm_server_poll(bm_server* srv, uint64_t ticket, int wait, bm_result* out);
@@ -232,6 +242,26 @@ int bm_server_stats(bm_server* srv, uint64_t* queued, uint64_t* running, double*
 void bm_server_destroy(bm_server* srv);
 /* Estimated device bytes one specimen of n voxels occupies while it runs. */
 uint64_t bm_footprint_bytes(size_t width, size_t height, size_t depth);
+
+/* ---- TIFF stacks ----------------------------------------------------------
+ * Reads a multi-page 8-bit grayscale TIFF as the reference's
+ * read_binary_tiff / read_roi_tiff do (tiff_io.rs:19-149): every page Gray(8)
+ * with the first page's dimensions; samples validated per `accepted`
+ * (BM_TIFF_ANY, BM_TIFF_ZERO_OR_255 = the strict-binary check,
+ * BM_TIFF_ROI_MASK = 0/1/255) and stored as (sample > threshold) ? 1 : 0,
+ * page after page (z), row after row (y), x fastest.  Uncompressed, PackBits,
+ * LZW and Deflate data, with or without horizontal differencing, strips or
+ * tiles, classic TIFF or BigTIFF, either byte order.  Pages are decoded in
+ * parallel straight into `out` (pass pinned host memory to copy it to the GPU
+ * without staging).  out == NULL: only the dimensions, of the pages before the
+ * first page that fails a structure check (page type, size); the decoding
+ * call reports that failure after validating the earlier pages' samples, in
+ * the reference's order.  Errors carry the reference's messages; read them with
+ * bm_last_error(NULL, ...).  BM_ERR_DIMS when a dimension is < 2
+ * (volume.rs:27-34). */
+enum { BM_TIFF_ANY = 0, BM_TIFF_ZERO_OR_255 = 1, BM_TIFF_ROI_MASK = 2 };
+int bm_tiff_read(const char* path, unsigned threshold, int accepted, uint8_t* out, size_t capacity,
+                 size_t* width, size_t* height, size_t* depth);
 
 /* Kernel launches issued by this context since creation (library kernels only). */
 uint64_t bm_ctx_launch_count(const bm_ctx* ctx);

@@ -80,3 +80,28 @@ def test_server_budget_admission():
     with Server(workers=1, hbm_budget_bytes=1e6) as srv:
         with pytest.raises(Exception, match="budget"):
             srv.submit(items[0].bone, items[0].roi, items[0].spacing_um)
+
+
+def test_server_tiff_requests(tmp_path, gpu_ctx):
+    """Requests read from TIFF stacks on the workers give the results of the
+    arrays they were written from; a missing ROI means every voxel, and a
+    decoding or shape error comes back in the result with its message."""
+    import tiffgen as T
+
+    sp = S.make_specimen((20, 36, 44), 2.5, 0.25, "cylinder", 16.0, 9.5, 61)
+    pb, pr = tmp_path / "b.tif", tmp_path / "r.tif"
+    T.write_tiff(pb, list(sp.bone), compression=T.DEFLATE, predictor=2)
+    T.write_tiff(pr, list(sp.roi), compression=T.PACKBITS, rows_per_strip=5)
+    bad_roi = tmp_path / "r2.tif"
+    T.write_tiff(bad_roi, list(sp.roi[:, :-1, :]))
+    ref = analyze_thickness((sp.bone > 0).astype(np.uint8), sp.roi, sp.spacing_um, ctx=gpu_ctx)
+    ref_all = analyze_thickness((sp.bone > 0).astype(np.uint8), np.ones_like(sp.roi), sp.spacing_um, ctx=gpu_ctx)
+    with Server(workers=2, hbm_budget_bytes=8e9) as srv:
+        t1 = srv.submit_tiff(pb, pr, sp.spacing_um, strict_binary=True)
+        t2 = srv.submit_tiff(pb, None, sp.spacing_um)
+        t3 = srv.submit_tiff(pb, bad_roi, sp.spacing_um)
+        r1, r2, r3 = srv.result(t1), srv.result(t2), srv.result(t3)
+    assert r1.status == 0 and r1.thickness.mean == ref.thickness.mean and r1.spacing.mean == ref.spacing.mean
+    assert r2.status == 0 and r2.spacing.standard_deviation == ref_all.spacing.standard_deviation
+    assert r3.status != 0
+    assert r3.message == "binary image dimensions 44x36x20 do not match ROI dimensions 44x35x20"
