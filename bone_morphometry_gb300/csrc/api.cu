@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "exact_sum.h"
@@ -574,6 +575,18 @@ int volume_metrics_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi
   return BM_OK;
 }
 
+// The context's twin (created on first use, with the parent's profiling state).
+bm_ctx* twin_of(bm_ctx* ctx) {
+  if (!ctx->inputs_ready) check(ctx, cudaEventCreateWithFlags(&ctx->inputs_ready, cudaEventDisableTiming), "event");
+  if (ctx->twin) return ctx->twin;
+  bm_ctx* t = nullptr;
+  const int st = bm_ctx_create(ctx->device, &t);
+  if (st != BM_OK) fail(ctx, st, "second stream context creation failed");
+  t->profiling = ctx->profiling;
+  ctx->twin = t;
+  return t;
+}
+
 int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, Dims dm, double spacing,
                      unsigned flags, bm_stats* th, bm_stats* sp, float* d_thmap, float* d_spmap, cudaStream_t s) {
   // metrics.rs:70-78
@@ -605,14 +618,46 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
   float* qm = nullptr;
   if (want_q && (!d_thmap || !d_spmap))
     qm = static_cast<float*>(ensure(ctx, ctx->qmap, (size_t)N * 4, "quantile map"));
+  // The two phases are independent: the marrow phase runs on the twin context
+  // (its own stream and buffers, on a second host thread) while this thread
+  // runs the bone phase, so their kernels overlap on the GPU.  Results and
+  // errors are reported in the reference's order (bone first).
+  bm_ctx* tw = twin_of(ctx);
   PhaseResult rb, rm;
   float* mb = d_thmap ? d_thmap : qm;
-  run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, s, rb);
+  float* mm = d_spmap ? d_spmap
+                      : (want_q ? static_cast<float*>(ensure(tw, tw->qmap, (size_t)N * 4, "quantile map")) : nullptr);
+  check(ctx, cudaEventRecord(ctx->inputs_ready, s), "event record");
+  int twin_status = BM_OK;
+  std::thread marrow([&] {
+    try {
+      cudaSetDevice(tw->device);
+      check(tw, cudaStreamWaitEvent(tw->stream, ctx->inputs_ready, 0), "stream wait");
+      run_phase(tw, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, tw->stream, rm);
+    } catch (const CallError& e) {
+      twin_status = e.status;
+    } catch (const std::bad_alloc&) {
+      tw->last_error = "host allocation failed";
+      twin_status = BM_ERR_OOM;
+    }
+  });
+  int bone_status = BM_OK;
+  try {
+    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, s, rb);
+  } catch (const CallError& e) {
+    bone_status = e.status;
+  }
+  marrow.join();
+  ctx->launches += tw->launches;
+  tw->launches = 0;
+  if (bone_status != BM_OK) throw CallError{bone_status};
   int st = finish_stats(ctx, rb.acc, th);
   if (st) return st;
   if (want_q && th) quantiles(ctx, mb, N, rb.acc.count, spacing, th, s);
-  float* mm = d_spmap ? d_spmap : qm;
-  run_phase(ctx, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, s, rm);
+  if (twin_status != BM_OK) {
+    ctx->last_error = tw->last_error;
+    throw CallError{twin_status};
+  }
   st = finish_stats(ctx, rm.acc, sp);
   if (st) return st;
   if (want_q && sp) quantiles(ctx, mm, N, rm.acc.count, spacing, sp, s);
@@ -640,6 +685,7 @@ size_t cached_bytes(const bm_ctx* ctx) {
                          &ctx->qhist,    &ctx->qtargets,   &ctx->qmap,       &ctx->rgeo};
   size_t t = 0;
   for (const Buffer* b : all) t += b->bytes;
+  if (ctx->twin) t += cached_bytes(ctx->twin);
   return t;
 }
 }  // namespace bm
@@ -679,6 +725,7 @@ int bm_ctx_create(int device, bm_ctx** out) {
 int bm_ctx_trim(bm_ctx* ctx) {
   return guarded(ctx, [&]() -> int {
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->twin) bm_ctx_trim(ctx->twin);
     Buffer* all[] = {&ctx->in_a,  &ctx->in_b,      &ctx->dist,       &ctx->dist2,      &ctx->stack,
                      &ctx->fillmap, &ctx->selbits,  &ctx->posbits,   &ctx->ridges,     &ctx->accum,      &ctx->cpart,
                      &ctx->outmap, &ctx->outmap2,  &ctx->occ,       &ctx->rank,       &ctx->rvals,
@@ -700,6 +747,9 @@ void bm_ctx_destroy(bm_ctx* ctx) {
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->twin) bm_ctx_destroy(ctx->twin);
+    ctx->twin = nullptr;
+    if (ctx->inputs_ready) cudaEventDestroy(ctx->inputs_ready);
     Buffer* all[] = {&ctx->lut,      &ctx->in_a,      &ctx->in_b,       &ctx->dist,     &ctx->dist2,
                      &ctx->stack,    &ctx->fillmap,   &ctx->selbits,    &ctx->posbits,  &ctx->ridges,
                      &ctx->counters, &ctx->accum,     &ctx->cpart,     &ctx->outmap,     &ctx->outmap2,  &ctx->host_pinned,
@@ -763,6 +813,7 @@ int bm_profile_enable(bm_ctx* ctx, int on) {
       }
     }
     ctx->profiling = on != 0;
+    if (ctx->twin) bm_profile_enable(ctx->twin, on);
     return BM_OK;
   });
 }
@@ -770,6 +821,17 @@ int bm_profile_enable(bm_ctx* ctx, int on) {
 int bm_profile_read(bm_ctx* ctx, bm_kernel_time* out, size_t cap, size_t* count) {
   return guarded(ctx, [&]() -> int {
     fold_profile(ctx);
+    if (ctx->twin) {  // the twin's kernels count as this context's
+      bm_ctx* t = ctx->twin;
+      std::lock_guard<std::mutex> tl(t->mu);
+      fold_profile(t);
+      for (int i = 0; i < KF_COUNT; ++i) {
+        ctx->prof_ms[i] += t->prof_ms[i];
+        ctx->prof_n[i] += t->prof_n[i];
+        t->prof_ms[i] = 0.0;
+        t->prof_n[i] = 0;
+      }
+    }
     size_t n = 0;
     for (int i = 0; i < KF_COUNT; ++i) {
       if (out && n < cap) {

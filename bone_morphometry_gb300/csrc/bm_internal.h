@@ -120,6 +120,10 @@ void pool_destroy(Pool* p);
 struct bm_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // second context (own stream and buffers) that runs the marrow phase of
+  // bm_tbth_tbsp while this one runs the bone phase; created on first use
+  bm_ctx* twin = nullptr;
+  cudaEvent_t inputs_ready = nullptr;
   std::mutex mu;
   std::string last_error;
   unsigned long long launches = 0;
