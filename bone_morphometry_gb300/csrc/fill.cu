@@ -209,13 +209,14 @@ constexpr int kBinChunk = 256;    // bins whose offsets are staged in shared mem
 constexpr int kEntWin = 768;      // ball entries staged in shared memory at a time
 constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself)
 constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
+constexpr int kRotStride = 33;    // words per range-OR row: lanes testing different planes hit different banks
 constexpr int kItems = 1024;      // (ball, plane) paint items per round
 constexpr int kHxMax = 31;        // balls up to this radius read their chord half-widths from a table
 constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
 
-// rot[lv - 1][z][y] = OR of the unpainted-voxel masks of rows y .. y + 2^lv - 1
-// of plane z (rows past the tile edge count as empty), lv = 1 .. 5.  Built
-// with shuffles, one plane per warp step.
+// rot[lv - 1][z][y] (rows of kRotStride words) = OR of the unpainted-voxel
+// masks of rows y .. y + 2^lv - 1 of plane z (rows past the tile edge count
+// as empty), lv = 1 .. 5.  Built with shuffles, one plane per warp step.
 __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uint32_t* __restrict__ rot, int warp,
                                           int lane, int nwarps) {
   for (int zz = warp; zz < kFillTZ; zz += nwarps) {
@@ -224,7 +225,7 @@ __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uin
     for (int lv = 1; lv < kRotLevels; ++lv) {
       const uint32_t u = __shfl_down_sync(0xffffffffu, v, 1 << (lv - 1));
       v |= (lane + (1 << (lv - 1)) < 32) ? u : 0u;
-      rot[((lv - 1) * kFillTZ + zz) * 32 + lane] = v;
+      rot[((lv - 1) * kFillTZ + zz) * kRotStride + lane] = v;
     }
   }
 }
@@ -236,9 +237,9 @@ __device__ __forceinline__ int vidx(int row, int x) {
   return row * 32 + (((((x >> 1) ^ (row & 15)) << 1)) | (x & 1));
 }
 
-constexpr size_t kTileFillSmemWords =
-    (size_t)kRows * 16 + kRows + (kBinChunk + 4) + kBinChunk + kEntWin + (kRotLevels - 1) * kFillTZ * 32 + kItems +
-    130 + (kHxMax + 1) * (kHxMax + 1) / 4;
+constexpr size_t kTileFillSmemWords = (size_t)kRows * 16 + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
+                                      (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130 +
+                                      (kHxMax + 1) * (kHxMax + 1) / 4;
 
 // One CTA per tile (32 x 32 x 16 voxels) paints the tile's selected voxels.
 // Shared memory:
@@ -273,8 +274,8 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
   uint32_t* boff = usel + kRows;                             // kBinChunk + 1
   uint32_t* nzb = boff + kBinChunk + 4;                      // kBinChunk
   uint32_t* ent = nzb + kBinChunk;                           // kEntWin
-  uint32_t* rot = ent + kEntWin;                             // (kRotLevels - 1) * kFillTZ * 32
-  uint32_t* item = rot + (kRotLevels - 1) * kFillTZ * 32;    // kItems
+  uint32_t* rot = ent + kEntWin;                             // (kRotLevels - 1) * kFillTZ * kRotStride
+  uint32_t* item = rot + (kRotLevels - 1) * kFillTZ * kRotStride;  // kItems
   uint16_t* hyt = reinterpret_cast<uint16_t*>(item + kItems);              // 257 (+1) half-words
   uint8_t* hxt = reinterpret_cast<uint8_t*>(item + kItems + 130);         // (kHxMax + 1)^2 bytes
   __shared__ uint32_t s_nnz, s_wlo, s_whi;
@@ -406,7 +407,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
                   if (lv == 0) {
                     orr = usel[zz * kFillTY + pya];
                   } else {
-                    const uint32_t* tl = rot + ((lv - 1) * kFillTZ + zz) * 32;
+                    const uint32_t* tl = rot + ((lv - 1) * kFillTZ + zz) * kRotStride;
                     orr = tl[pya] | tl[pyb - (1 << lv) + 1];
                   }
                   pass = (orr & range_mask(xa, xb)) != 0u;
