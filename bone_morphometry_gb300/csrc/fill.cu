@@ -382,51 +382,54 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
           }
           const uint32_t se = min(min(e, s_whi), ss + (uint32_t)kRound);
           const uint32_t wb = ss - s_wlo;  // window index of the round's first ball
-          // test: two balls per warp, lanes 0..15 on ball 2w, lanes 16..31 on ball 2w+1
-          for (uint32_t bp = 2 * warp; bp < se - ss; bp += 2 * kFillWarps) {
-            const uint32_t bi = bp + half;
+          // test: four balls per warp step, two per half-warp (lanes 0..15 on
+          // balls 4w and 4w+2, lanes 16..31 on 4w+1 and 4w+3); lane hl tests
+          // plane zlo + hl of each.  Written without branches so that the two
+          // balls' tests interleave.
+          auto plane_test = [&](uint32_t bi, int& pya, int& pyb, int& zz) -> bool {
             const bool have = bi < se - ss;
-            const uint32_t c = have ? ent[wb + bi] : 0u;
+            const uint32_t c = ent[wb + (have ? bi : 0u)];
             const int cx = (int)(c & 0x3ffu) - 512, cy = (int)((c >> 10) & 0x3ffu) - 512, cz = (int)(c >> 20) - 512;
             const int zlo = max(cz - rad, 0), zhi = min(cz + rad, vz - 1);
-            const int zz = zlo + hl;
-            bool pass = false;
-            int pya = 0, pyb = 0;  // the disk's rows inside the tile
-            if (have && zz <= zhi) {
-              const int dz = zz - cz;
-              const int prem = R - dz * dz;
-              if (prem >= 0) {
-                const int hy = (int)hyt[abs(dz)];
-                pya = max(cy - hy, 0);
-                pyb = min(cy + hy, vy - 1);
-                const int xa = max(cx - hy, 0), xb = min(cx + hy, vx - 1);
-                if (pya <= pyb && xa <= xb) {
-                  const int span = pyb - pya + 1;
-                  const int lv = 31 - __clz(span);  // 2^lv <= span
-                  uint32_t orr;
-                  if (lv == 0) {
-                    orr = usel[zz * kFillTY + pya];
-                  } else {
-                    const uint32_t* tl = rot + ((lv - 1) * kFillTZ + zz) * kRotStride;
-                    orr = tl[pya] | tl[pyb - (1 << lv) + 1];
-                  }
-                  pass = (orr & range_mask(xa, xb)) != 0u;
-                }
-              }
-            }
-            // items: (window index, rows ya .. ya + n - 1, plane); planes of at
-            // most 16 rows go to the half-warp list at the top of the array
+            zz = zlo + hl;
+            const int dz = zz - cz;
+            bool ok = have && zz <= zhi;  // then |dz| <= rad
+            const int hy = (int)hyt[min(abs(dz), rad)];
+            pya = max(cy - hy, 0);
+            pyb = min(cy + hy, vy - 1);
+            const int xa = max(cx - hy, 0), xb = min(cx + hy, vx - 1);
+            ok = ok && pya <= pyb && xa <= xb;
+            const int zc = min(zz, kFillTZ - 1);
+            const int ya = min(pya, 31), yb = max(min(pyb, 31), ya);
+            const int lv = 31 - __clz(yb - ya + 1);  // 2^lv <= span
+            const uint32_t* tl = rot + (max(lv - 1, 0) * kFillTZ + zc) * kRotStride;
+            const uint32_t orr = lv == 0 ? usel[zc * kFillTY + ya] : (tl[ya] | tl[yb - (1 << lv) + 1]);
+            return ok && (orr & range_mask(min(max(xa, 0), 31), max(min(xb, 31), min(max(xa, 0), 31)))) != 0u;
+          };
+          // items: (window index, rows ya .. ya + n - 1, plane); planes of at
+          // most 16 rows go to the half-warp list at the top of the array
+          auto append = [&](uint32_t bi, bool pass, int pya, int pyb, int zz) {
             const bool wide = pass && pyb - pya >= 16;
             const unsigned act_w = __ballot_sync(0xffffffffu, wide);
             const unsigned act_n = __ballot_sync(0xffffffffu, pass && !wide);
             if (act_w | act_n) {
               uint32_t base = 0;
-              if (lane == 0) base = atomicAdd(&s_nitem[parity], (uint32_t)__popc(act_w) | ((uint32_t)__popc(act_n) << 16));
+              if (lane == 0)
+                base = atomicAdd(&s_nitem[parity], (uint32_t)__popc(act_w) | ((uint32_t)__popc(act_n) << 16));
               base = __shfl_sync(0xffffffffu, base, 0);
-              const uint32_t q = ((wb + bi) << 14) | ((uint32_t)(pyb - pya) << 9) | ((uint32_t)pya << 4) | (uint32_t)zz;
+              const uint32_t q =
+                  ((wb + bi) << 14) | ((uint32_t)(pyb - pya) << 9) | ((uint32_t)pya << 4) | (uint32_t)zz;
               if (wide) item[(base & 0xffffu) + __popc(act_w & lanes_below)] = q;
               else if (pass) item[kItems - 1 - ((base >> 16) + __popc(act_n & lanes_below))] = q;
             }
+          };
+          for (uint32_t bp = 4 * warp; bp < se - ss; bp += 4 * kFillWarps) {
+            const uint32_t b1 = bp + half, b2 = bp + 2 + half;
+            int ya1, yb1, z1, ya2, yb2, z2;
+            const bool p1 = plane_test(b1, ya1, yb1, z1);
+            const bool p2 = plane_test(b2, ya2, yb2, z2);
+            append(b1, p1, ya1, yb1, z1);
+            append(b2, p2, ya2, yb2, z2);
           }
           __syncthreads();
           // paint: the round's items over all warps, one row per lane (wide
