@@ -130,6 +130,7 @@ SIGNATURES = {
                              ctypes.POINTER(ctypes.c_double)]),
     "bm_server_destroy": (None, [_vp]),
     "bm_footprint_bytes": (ctypes.c_uint64, [_sz, _sz, _sz]),
+    "bm_ctx_set_concurrent_phases": (_i, [_vp, _i]),
     "bm_tiff_read": (_i, [ctypes.c_char_p, ctypes.c_uint, _i, _vp, _sz, ctypes.POINTER(_sz), ctypes.POINTER(_sz),
                           ctypes.POINTER(_sz)]),
 }
@@ -208,6 +209,10 @@ class Context:
     def profile(self, on: bool = True) -> None:
         """Start (clearing totals) or stop CUDA-event timing of library kernels."""
         self.call("bm_profile_enable", 1 if on else 0)
+
+    def set_concurrent_phases(self, on: bool = True) -> None:
+        """Tb.Th and Tb.Sp side by side on two streams (default) or one after the other."""
+        self.call("bm_ctx_set_concurrent_phases", 1 if on else 0)
 
     def kernel_times(self) -> dict:
         """{family: (launches, total_ms)} of the kernels timed since profile(True)."""

@@ -68,6 +68,8 @@ constexpr int kFillTZ = 16;
 // Largest r^2 whose sphere lattice points the tile fill tabulates (radius 256);
 // volumes with larger distances use the per-ball atomic fill.
 constexpr uint32_t kSurfMaxR2 = 65536;
+// Largest volume whose Tb.Th and Tb.Sp phases run side by side (bm_tbth_tbsp).
+constexpr long long kSplitMaxVoxels = 1ll << 28;
 
 // Device-side sizes of one phase's fill binning.
 struct FillInfo {
@@ -124,6 +126,7 @@ struct bm_ctx {
   // bm_tbth_tbsp while this one runs the bone phase; created on first use
   bm_ctx* twin = nullptr;
   cudaEvent_t inputs_ready = nullptr;
+  bool split_phases = true;  // false: both phases on this context, one after the other
   std::mutex mu;
   std::string last_error;
   unsigned long long launches = 0;

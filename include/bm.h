@@ -263,6 +263,15 @@ enum { BM_TIFF_ANY = 0, BM_TIFF_ZERO_OR_255 = 1, BM_TIFF_ROI_MASK = 2 };
 int bm_tiff_read(const char* path, unsigned threshold, int accepted, uint8_t* out, size_t capacity,
                  size_t* width, size_t* height, size_t* depth);
 
+/* Tb.Th and Tb.Sp of bm_tbth_tbsp run side by side by default for volumes of
+ * up to 2^28 voxels: the marrow phase on a second internal context (its own
+ * stream and buffers, about doubling the per-phase device memory) while the
+ * bone phase runs; larger volumes fill the GPU with one phase and run them one
+ * after the other.  on == 0 always runs them one after the other on this
+ * context (each kernel then has the GPU to itself, e.g. to time kernels
+ * alone).  Results are identical either way. */
+int bm_ctx_set_concurrent_phases(bm_ctx* ctx, int on);
+
 /* Kernel launches issued by this context since creation (library kernels only). */
 uint64_t bm_ctx_launch_count(const bm_ctx* ctx);
 

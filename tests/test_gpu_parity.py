@@ -214,3 +214,23 @@ def test_device_tensor_path(gpu_ctx):
     vol = torch.from_numpy(O.phase_inside(sp.bone, sp.roi, True)).cuda()
     e = euclidean_distance_transform_squared(vol, ctx=gpu_ctx).cpu().numpy().view(np.uint32)
     assert np.array_equal(e, O.edt_sq(vol.cpu().numpy()))
+
+
+def test_phases_side_by_side_or_sequential_agree(gpu_ctx):
+    """Tb.Th / Tb.Sp with the two phases on two streams (default) and one after
+    the other: identical maps and statistics, quantiles included."""
+    sp = S.make_specimen((30, 44, 52), 2.5, 0.3, "cylinder", 19.0, 13.0, 71)
+    from bone_morphometry_gb300 import FeatureMode
+    a = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx, return_maps=True,
+                          feature_mode=FeatureMode.STANDARD)
+    gpu_ctx.set_concurrent_phases(False)
+    try:
+        b = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx, return_maps=True,
+                              feature_mode=FeatureMode.STANDARD)
+    finally:
+        gpu_ctx.set_concurrent_phases(True)
+    assert np.array_equal(a.thickness_map.view(np.uint32), b.thickness_map.view(np.uint32))
+    assert np.array_equal(a.spacing_map.view(np.uint32), b.spacing_map.view(np.uint32))
+    for x, y in ((a.thickness, b.thickness), (a.spacing, b.spacing)):
+        assert x.mean == y.mean and x.standard_deviation == y.standard_deviation and x.median == y.median
+        assert x.percentile_90 == y.percentile_90
