@@ -311,7 +311,7 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   uint32_t* occ = static_cast<uint32_t*>(ensure(ctx, ctx->occ, rwords * 4, "r2 flags"));
   check(ctx, cudaMemsetAsync(occ, 0, rwords * 4, s), "memset");
   timed(ctx, KF_RIDGE, s, "ridge kernel",
-        [&] { return launch_ridges(E, dm, lut, ridges, ctr, occ, s, &ctx->launches); });
+        [&] { return launch_ridges(E, selbits, dm, lut, ridges, ctr, occ, s, &ctx->launches); });
   uint32_t* F = d_sq ? d_sq : B;
   fill_phase(ctx, dm, ridges, ctr, res.selected, hc.rmax, occ, selbits, F, s);
   StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));

@@ -312,13 +312,22 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       s_nitem[1] = 0u;
     }
     parity = 0;
+    bool any_sel = false;
     for (int r = tid; r < kRows; r += kFillThreads) {
       const int zz = r / kFillTY, yy = r % kFillTY;
       uint32_t own = 0u;
       if (zz < vz && yy < vy) own = selbits[((long long)(z0 + zz) * dm.h + (y0 + yy)) * nw + tx] & xmask;
       usel[r] = own;
+      any_sel = any_sel || own != 0u;
     }
-    __syncthreads();
+    if (!__syncthreads_or(any_sel)) {  // nothing selected here (outside the ROI, say): all zero
+      for (int r = warp; r < kRows; r += kFillWarps) {
+        const int zz = r / kFillTY, yy = r % kFillTY;
+        if (zz < vz && yy < vy && lane < vx)
+          fillmap[((long long)(z0 + zz) * dm.h + (y0 + yy)) * dm.w + x0 + lane] = 0u;
+      }
+      continue;
+    }
     build_rot(usel, rot, warp, lane, kFillWarps);
     for (uint32_t b0 = 0; b0 < nR; b0 += kBinChunk) {
       const uint32_t nb = min((uint32_t)kBinChunk, nR - b0);

@@ -44,7 +44,7 @@ cudaError_t launch_lut(uint4* lut, uint32_t lo, uint32_t hi, cudaStream_t s, uns
 
 // Distance-ridge extraction: appends {linear index, r2} records and, when occ
 // is not null, sets occ[r2] = 1 for every ridge r2.
-cudaError_t launch_ridges(const uint32_t* dist, Dims dm, const uint4* lut, uint2* ridges,
+cudaError_t launch_ridges(const uint32_t* dist, const uint32_t* selbits, Dims dm, const uint4* lut, uint2* ridges,
                           Counters* ctr, uint32_t* occ, cudaStream_t s, unsigned long long* launches);
 
 // Sphere fill: atomic max of r2 over every voxel of each ridge ball (any phase).

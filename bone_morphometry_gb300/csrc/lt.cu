@@ -199,7 +199,22 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
     const int x0 = tx * kCTX, y0 = ty * kCTY, z0 = tz * kCTZ;
-    __syncthreads();
+    // a tile without selected voxels (outside the ROI, say) has a zero output and
+    // no statistics: skip its staging
+    bool any_sel = false;
+    if (tid < kCTZ * kCTY) {
+      const int z = z0 + tid / kCTY, y = y0 + tid % kCTY;
+      if (z < dm.d && y < dm.h) any_sel = selbits[((long long)z * dm.h + y) * nw + tx] != 0u;
+    }
+    if (!__syncthreads_or(any_sel)) {
+      if (outmap) {
+        for (int r = warp; r < kCTZ * kCTY; r += kCleanThreads / 32) {
+          const int z = z0 + r / kCTY, y = y0 + r % kCTY, x = x0 + lane;
+          if (z < dm.d && y < dm.h && x < dm.w) outmap[((long long)z * dm.h + y) * dm.w + x] = 0.0f;
+        }
+      }
+      continue;
+    }
     // stage the r^2 map with halo 2: one row of 36 per warp step.  Each warp
     // has 18 rows; their loads are issued in batches of 3 before any use, so
     // the latencies overlap.
@@ -360,18 +375,25 @@ constexpr int kRTX = 32, kRTY = 8, kRTZ = 8;
 constexpr int kRSX = kRTX + 2, kRSY = kRTY + 2, kRSZ = kRTZ + 2;
 
 __global__ void __launch_bounds__(256)
-ridge_tile_kernel(const uint32_t* __restrict__ dist, Dims dm, const uint4* __restrict__ lut,
-                  uint2* __restrict__ ridges, Counters* __restrict__ ctr, uint32_t* __restrict__ occ, int ntx,
-                  int nty, int ntz) {
+ridge_tile_kernel(const uint32_t* __restrict__ dist, const uint32_t* __restrict__ selbits, Dims dm,
+                  const uint4* __restrict__ lut, uint2* __restrict__ ridges, Counters* __restrict__ ctr,
+                  uint32_t* __restrict__ occ, int ntx, int nty, int ntz) {
   __shared__ uint32_t D[kRSZ * kRSY * kRSX];
   __shared__ uint32_t s_wcnt[8];
   __shared__ unsigned long long s_base;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long ntiles = (long long)ntx * nty * ntz;
+  const int nw = dm.nw();
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
     const int x0 = tx * kRTX, y0 = ty * kRTY, z0 = tz * kRTZ;
-    __syncthreads();
+    // ridges are selected voxels: a tile without any has none
+    bool any_sel = false;
+    if (tid < kRTZ * kRTY) {
+      const int z = z0 + tid / kRTY, y = y0 + tid % kRTY;
+      if (z < dm.d && y < dm.h) any_sel = selbits[((long long)z * dm.h + y) * nw + tx] != 0u;
+    }
+    if (!__syncthreads_or(any_sel)) continue;
     // stage the distance map with halo 1: one row of 34 per warp step, loads
     // of all the warp's rows issued before the stores
     constexpr int kRidgeRows = (kRSZ * kRSY + 7) / 8;  // 13 (the last step covers 4 rows)
@@ -489,12 +511,12 @@ cudaError_t launch_dia_table(const uint4* lut, uint32_t n, float* dia, cudaStrea
   return cudaGetLastError();
 }
 
-cudaError_t launch_ridges(const uint32_t* dist, Dims dm, const uint4* lut, uint2* ridges, Counters* ctr,
-                          uint32_t* occ, cudaStream_t s, unsigned long long* launches) {
+cudaError_t launch_ridges(const uint32_t* dist, const uint32_t* selbits, Dims dm, const uint4* lut, uint2* ridges,
+                          Counters* ctr, uint32_t* occ, cudaStream_t s, unsigned long long* launches) {
   const int ntx = (dm.w + kRTX - 1) / kRTX, nty = (dm.h + kRTY - 1) / kRTY, ntz = (dm.d + kRTZ - 1) / kRTZ;
   const long long tiles = (long long)ntx * nty * ntz;
-  ridge_tile_kernel<<<resident_grid(ridge_tile_kernel, 256, 0, tiles), 256, 0, s>>>(dist, dm, lut, ridges, ctr, occ,
-                                                                                    ntx, nty, ntz);
+  ridge_tile_kernel<<<resident_grid(ridge_tile_kernel, 256, 0, tiles), 256, 0, s>>>(dist, selbits, dm, lut, ridges,
+                                                                                    ctr, occ, ntx, nty, ntz);
   ++*launches;
   return cudaGetLastError();
 }
