@@ -306,7 +306,7 @@ def bench_batch(ctx, n_items=64):
             "data": "torch GPU generator, sizes log-uniform [96,384] per axis"}
 
 
-def bench_serving(n_requests=64, rate=200.0, budget=120e9, workers=(1, 2, 4)):
+def bench_serving(n_requests=64, rate=200.0, budget=120e9, workers=(2, 4)):
     """Poisson arrivals (rate req/s) of specimens with edges log-uniform in
     [64, 768]; 24 distinct generated specimens are cycled.  Served form
     (continuous admission, HBM budget) vs serial plain processing of the same
@@ -338,7 +338,8 @@ def bench_serving(n_requests=64, rate=200.0, budget=120e9, workers=(1, 2, 4)):
         alone.append(analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=ctx))
         service.append(time.perf_counter() - t0)
     ctx.close()
-    # serial plain: one request at a time in arrival order
+    # ideal serial queue (each request's service time measured alone, no
+    # overheads between requests), for reference
     t_arr = np.cumsum(gaps)
     end = 0.0
     lat_serial = []
@@ -360,30 +361,35 @@ def bench_serving(n_requests=64, rate=200.0, budget=120e9, workers=(1, 2, 4)):
                 tickets.append((k, srv.submit(pool[k].bone, pool[k].roi, pool[k].spacing_um)))
             return [(k, srv.result(t)) for k, t in tickets]
 
-    # worker count: the same arrival sequence served with each candidate; the
-    # lowest p99 is reported (the others are listed)
+    # serial plain, measured: one request at a time in arrival order (a single
+    # worker).  Served: the same arrival sequence with several workers; the
+    # worker count with the lowest p99 is reported (all are listed)
     runs = {}
-    for nworkers in workers:
+    for nworkers in (1,) + tuple(w for w in workers if w != 1):
         res_w = serve(nworkers)
         lat_w = [r.latency_s for _, r in res_w]
         runs[nworkers] = (percentile(lat_w, 0.99), res_w)
-    best = min(runs, key=lambda k: runs[k][0])
+    best = min((k for k in runs if k != 1), key=lambda k: runs[k][0])
     results = runs[best][1]
-    first = min(r.submit_s for _, r in results)
-    last = max(r.end_s for _, r in results)
-    lat = [r.latency_s for _, r in results]
     vox = sum(int(pool[k].bone.size) for k in order)
+
+    def summary(res):
+        first = min(r.submit_s for _, r in res)
+        last = max(r.end_s for _, r in res)
+        lat = [r.latency_s for _, r in res]
+        return vox / (last - first) / 1e9, 1e3 * percentile(lat, 0.5), 1e3 * percentile(lat, 0.99)
+
+    served = summary(results)
+    serial = summary(runs[1][1])
     same = all(r.status == 0 and r.thickness.mean == alone[k].thickness.mean
                and r.spacing.standard_deviation == alone[k].spacing.standard_deviation
                for res_w in (v[1] for v in runs.values()) for k, r in res_w)
     return {"requests": n_requests, "offered_req_s": rate, "distinct_specimens": len(pool),
             "mean_voxels_per_request": vox / n_requests, "hbm_budget_gb": budget / 1e9, "workers": best,
             "p99_ms_by_workers": {str(k): round(1e3 * v[0], 2) for k, v in runs.items()},
-            "served_gvoxel_s": vox / (last - first) / 1e9,
-            "served_p50_ms": 1e3 * percentile(lat, 0.5), "served_p99_ms": 1e3 * percentile(lat, 0.99),
-            "serial_plain_gvoxel_s": vox / span_serial / 1e9,
-            "serial_plain_p50_ms": 1e3 * percentile(lat_serial, 0.5),
-            "serial_plain_p99_ms": 1e3 * percentile(lat_serial, 0.99),
+            "served_gvoxel_s": served[0], "served_p50_ms": served[1], "served_p99_ms": served[2],
+            "serial_plain_gvoxel_s": serial[0], "serial_plain_p50_ms": serial[1], "serial_plain_p99_ms": serial[2],
+            "serial_ideal_p99_ms": 1e3 * percentile(lat_serial, 0.99),
             "results_identical_to_alone": bool(same),
             "data": "torch GPU generator, edges log-uniform [64,768]; host-pointer requests (H2D inside)"}
 
