@@ -309,8 +309,10 @@ def bench_batch(ctx, n_items=64):
 def bench_serving(n_requests=64, rate=200.0, budget=120e9, workers=(2, 4)):
     """Poisson arrivals (rate req/s) of specimens with edges log-uniform in
     [64, 768]; 24 distinct generated specimens are cycled.  Served form
-    (continuous admission, HBM budget) vs serial plain processing of the same
-    arrival sequence (queueing computed from each specimen's measured plain time)."""
+    (continuous admission, HBM budget, several workers) vs serial plain
+    processing of the same arrival sequence (one request at a time, measured),
+    plus the p99 of an ideal serial queue built from each specimen's service
+    time measured alone."""
     import numpy as np
     import torch
 
