@@ -150,7 +150,7 @@ struct bm_ctx {
   bm::Buffer outmap2;
   bm::Buffer host_pinned;      // pinned staging for small readbacks
   bm::Buffer occ, rank, rvals; // per-r^2 flags, ranks, rank -> r^2
-  bm::Buffer rgeo;             // rank -> {r^2, ceil sqrt, floor sqrt, sphere-table z base}
+  bm::Buffer rgeo;             // rank -> {r^2, ceil sqrt, floor sqrt, 0}
   bm::Buffer fillinfo;         // bm::FillInfo
   bm::Buffer bincounts, binoffsets, binentries, scanscratch;
   // cached sphere lattice-point table for r2 in [0, surf_max]

@@ -2,16 +2,24 @@
 //
 // The reference paints every voxel of every ridge ball with an atomic max:
 // sum over ridges of |ball| operations (~7e10 for a 512^3 marrow phase, where
-// every voxel is covered ~500 times).  Here the output volume is cut into
-// 32x32x16 tiles, each owned by one CTA that paints its tile in shared memory.
-// The balls that reach a tile are visited in strictly descending r^2 (a
-// counting sort by (tile, r^2 rank)); the final value of a voxel is the r^2 of
-// the first -- largest -- ball that covers it, so a per-row bitmask of
-// still-unpainted voxels lets every later ball skip whatever is already
-// decided.  Balls of equal r^2 paint the same value and run concurrently; a
-// barrier separates consecutive r^2 groups.  The result is the reference's
-// max-of-balls map bit for bit, with ~one shared-memory store per voxel plus
-// one mask test per (ball, row) instead of one global atomic per (ball, voxel).
+// every voxel is covered ~500 times).  Here the work splits in two:
+//
+// Selected voxels: the output volume is cut into 32x32x16 tiles, each owned by
+// one CTA that paints its tile in shared memory.  The balls that reach a tile
+// are visited in strictly descending r^2 (a counting sort by (tile, r^2
+// rank)); the final value of a voxel is the r^2 of the first -- largest --
+// ball that covers it, so per-row bitmasks of still-unpainted voxels let every
+// later ball skip whatever is already decided.  Balls of equal r^2 paint the
+// same value and run concurrently; a barrier separates consecutive r^2 groups.
+// Each group is processed in rounds: a plane test per (ball, plane) against a
+// range-OR table of the masks, then a load-balanced pass that paints the
+// chords of the planes that passed, one row per lane.
+//
+// Non-selected voxels: a ball reaches one only on its sphere (its r^2 is the
+// distance to the nearest non-selected voxel), so a per-ridge pass over the
+// sphere's lattice points adds those with an atomic max.
+//
+// The result is the reference's max-of-balls map bit for bit.
 //
 // Pipeline (one phase):
 //   ridge_tile_kernel  -> ridge records + occ[r2] flags
