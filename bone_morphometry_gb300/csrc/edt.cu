@@ -366,7 +366,7 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
   if (threadIdx.x == 0) s_need = 0u;
   __syncthreads();
   // centre rows (loads of the warp's 16 rows issued before their use)
-  uint32_t need = 0;
+  uint32_t need = 0;  // halo rows this block needs: from its largest finite value
   constexpr int kPer = kWinTL / kWinWarps;  // 16
   uint32_t f[kPer];
 #pragma unroll
@@ -374,15 +374,22 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
     const int q = q0 + warp + kWinWarps * j;
     f[j] = (xin && q < n) ? in[base + (long long)q * stride] : kInfSq;
   }
+  uint32_t fmax = 0;  // largest finite value (the halo bound grows with it)
+  bool inf = false;
 #pragma unroll
   for (int j = 0; j < kPer; ++j) {
     const uint32_t v = f[j];
-    if (v != 0u) need = max(need, v == kInfSq ? 0xffffu : halo_need(v));
+    inf = inf || v == kInfSq;
+    fmax = max(fmax, v == kInfSq ? 0u : v);
     buf[(kWinHalo + warp + kWinWarps * j) * 32 + lane] = v == kInfSq ? kBigSq : v;
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
-  if (lane == 0) atomicMax(&s_need, need);
+  for (int o = 16; o > 0; o >>= 1) fmax = max(fmax, __shfl_xor_sync(0xffffffffu, fmax, o));
+  inf = __any_sync(0xffffffffu, inf);
+  if (lane == 0) {
+    need = inf ? 0xffffu : (fmax ? halo_need(fmax) : 0u);
+    atomicMax(&s_need, need);
+  }
   __syncthreads();
   const int halo = (int)min(s_need, (uint32_t)kWinHalo);
   for (int i = warp; i < halo; i += kWinWarps) {
@@ -395,15 +402,17 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
   __syncthreads();
   uint32_t localmax = 0;
   bool bad = false;
+  uint32_t* op = out + base + (long long)(q0 + warp) * stride;  // output of row j, advanced per j
+  const long long ostep = (long long)kWinWarps * stride;
 #pragma unroll 1
-  for (int j = 0; j < kPer; ++j) {
+  for (int j = 0; j < kPer; ++j, op += ostep) {
     const int i = warp + kWinWarps * j;
     const int q = q0 + i;
     if (!xin || q >= n) continue;
     const uint32_t* col = buf + (kWinHalo + i) * 32 + lane;
     uint32_t best = col[0];
     if (best == 0u) {
-      out[base + (long long)q * stride] = 0u;
+      *op = 0u;
       continue;
     }
     // every p with |q - p| < dp has been tried once dp^2 >= best (a step
@@ -432,7 +441,7 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
       bad = true;
       continue;
     }
-    out[base + (long long)q * stride] = best;
+    *op = best;
     localmax = max(localmax, best);
   }
   if (bad) redo[orow * (long long)w + x] = 1u;
