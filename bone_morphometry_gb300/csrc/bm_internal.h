@@ -12,7 +12,9 @@
 
 namespace bm {
 
-constexpr uint32_t kInfSq = 0xFFFFFFFFu;  // "no site on this line" in the EDT passes
+// "No site on this line" in the EDT passes: larger than any squared distance
+// (< 2^31), yet adding a scan offset dp^2 (dp <= 67) to it cannot wrap.
+constexpr uint32_t kInfSq = 0xF0000000u;
 
 // Selection of the phase from the inputs, evaluated inside the first EDT pass
 // (edt.rs:19-24 and volume.rs:84-105).

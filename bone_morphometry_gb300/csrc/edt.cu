@@ -336,10 +336,7 @@ constexpr int kWinTL = 128;
 constexpr int kWinHalo = 64;
 constexpr int kWinThreads = 256;
 constexpr int kWinWarps = kWinThreads / 32;
-// "No site" inside the window kernel: larger than any real squared distance
-// (< 2^30 + 2^30) yet small enough that adding a staged offset dp^2 (dp <=
-// kWinHalo + 3) cannot wrap, so the scan needs no special case for it.
-constexpr uint32_t kBigSq = 0xF0000000u;
+static_assert(kInfSq + (kWinHalo + 3u) * (kWinHalo + 3u) > kInfSq, "the window scan adds dp^2 to kInfSq");
 
 // floor(sqrt(f)) + 2 >= isqrt(f - 1) + 1 for f >= 1: the halo that f needs,
 // from the hardware reciprocal square root (error far below one).
@@ -381,7 +378,7 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
     const uint32_t v = f[j];
     inf = inf || v == kInfSq;
     fmax = max(fmax, v == kInfSq ? 0u : v);
-    buf[(kWinHalo + warp + kWinWarps * j) * 32 + lane] = v == kInfSq ? kBigSq : v;
+    buf[(kWinHalo + warp + kWinWarps * j) * 32 + lane] = v;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) fmax = max(fmax, __shfl_xor_sync(0xffffffffu, fmax, o));
@@ -396,8 +393,8 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
     const int ql = q0 - 1 - i, qr = q0 + kWinTL + i;
     const uint32_t l = (xin && ql >= 0) ? in[base + (long long)ql * stride] : kInfSq;
     const uint32_t r = (xin && qr < n) ? in[base + (long long)qr * stride] : kInfSq;
-    buf[(kWinHalo - 1 - i) * 32 + lane] = l == kInfSq ? kBigSq : l;
-    buf[(kWinHalo + kWinTL + i) * 32 + lane] = r == kInfSq ? kBigSq : r;
+    buf[(kWinHalo - 1 - i) * 32 + lane] = l;
+    buf[(kWinHalo + kWinTL + i) * 32 + lane] = r;
   }
   __syncthreads();
   uint32_t localmax = 0;
