@@ -507,8 +507,13 @@ def run_gpu(args, rank, world, local):
         slices = args.cpu_sample_slices or default_slices(sp)
         vox, dt = cpu_sample_run(sp, slices, threads)
         d, h, w = sp.bone.shape
+        # one thread too, on a slab 1/8 as thick (the same algorithm, no parallelism)
+        slices1 = max(4, slices // 8)
+        vox1, dt1 = cpu_sample_run(sp, slices1, 1)
         cpu = {"value": vox / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "z-slab %dx%dx%d of the same specimen, both phases, %.1f s" % (w, h, slices, dt)}
+               "sample": "z-slab %dx%dx%d of the same specimen, both phases, %.1f s" % (w, h, slices, dt),
+               "value_1_thread": vox1 / dt1 / 1e9,
+               "sample_1_thread": "z-slab %dx%dx%d, both phases, %.1f s" % (w, h, slices1, dt1)}
 
     extras = {}
     if world == 1 and not args.no_extras:
