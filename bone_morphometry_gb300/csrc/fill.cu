@@ -36,10 +36,13 @@ namespace bm {
 
 namespace {
 
-// floor(sqrt(v)) for v < 2^30: the correctly rounded single-precision root is
-// within one of the answer, so one correction step each way makes it exact.
+// floor(sqrt(v)) for v < 2^30 from the hardware reciprocal square root: the
+// estimate (float)v * rsqrt((float)v) is within 0.01 of sqrt(v) there (the
+// float conversion and the reciprocal root are each within a few ulp), so one
+// integer correction step each way makes the floor exact.
 __device__ __forceinline__ uint32_t isqrt_u32(uint32_t v) {
-  uint32_t r = (uint32_t)sqrtf((float)v);
+  const float f = (float)v;
+  uint32_t r = (uint32_t)(f * rsqrtf(fmaxf(f, 1.0f)));
   r -= (r * r > v) ? 1u : 0u;
   r += ((r + 1) * (r + 1) <= v) ? 1u : 0u;
   return r;
@@ -50,16 +53,8 @@ __device__ __forceinline__ uint32_t csqrt_u32(uint32_t v) {
   return f * f == v ? f : f + 1;
 }
 
-// floor(sqrt(v)) for v < 2^24 from the hardware reciprocal square root: the
-// estimate v * rsqrt(v) is within far less than one of sqrt(v) there, so one
-// integer correction step each way makes the floor exact.
-__device__ __forceinline__ uint32_t isqrt24(uint32_t v) {
-  const float f = (float)v;
-  uint32_t r = (uint32_t)(f * rsqrtf(fmaxf(f, 1.0f)));
-  r -= (r * r > v) ? 1u : 0u;
-  r += ((r + 1) * (r + 1) <= v) ? 1u : 0u;
-  return r;
-}
+// The same floor square root where v < 2^24 is known.
+__device__ __forceinline__ uint32_t isqrt24(uint32_t v) { return isqrt_u32(v); }
 
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
