@@ -31,6 +31,47 @@ struct Dims {
   __host__ __device__ int nw() const { return (w + 31) >> 5; }  // 32-bit words per x row of a bitmask
 };
 
+// Unsigned 32-bit division by a fixed divisor d >= 2 through a multiply
+// (the round-up method of Granlund and Montgomery): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (t + ((n - t) >> 1)) >> (l - 1)
+// where t = mulhi(m, n), for every 32-bit n.
+struct FastDiv {
+  uint32_t d, m, s;
+  static FastDiv of(uint32_t div) {
+    FastDiv f;
+    f.d = div;
+    uint32_t l = 0;
+    while ((1ull << l) < div) ++l;
+    f.m = (uint32_t)(((1ull << 32) * ((1ull << l) - div)) / div + 1);
+    f.s = l - 1;
+    return f;
+  }
+#ifdef __CUDACC__
+  __device__ __forceinline__ uint32_t div(uint32_t n) const {
+    const uint32_t t = __umulhi(m, n);
+    return (t + ((n - t) >> 1)) >> s;
+  }
+#endif
+};
+
+// Linear voxel index -> (x, y, z) without hardware division.
+struct VoxelDecoder {
+  FastDiv w, wh;
+  static VoxelDecoder of(const Dims& dm) {
+    return VoxelDecoder{FastDiv::of((uint32_t)dm.w), FastDiv::of((uint32_t)dm.w * (uint32_t)dm.h)};
+  }
+#ifdef __CUDACC__
+  __device__ __forceinline__ void operator()(uint32_t idx, int& x, int& y, int& z) const {
+    const uint32_t zq = wh.div(idx);
+    const uint32_t rem = idx - zq * wh.d;
+    const uint32_t yq = w.div(rem);
+    z = (int)zq;
+    y = (int)yq;
+    x = (int)(rem - yq * w.d);
+  }
+#endif
+};
+
 // Exact-sum accumulator for the statistics: per f32 exponent the sum of the
 // 24-bit mantissas and of the 48-bit squared mantissas (split into two 24-bit
 // halves), plus count and maximum.  Exact for < 2^34 values.

@@ -131,13 +131,6 @@ struct Geom {
   long long ntiles;
 };
 
-__device__ __forceinline__ void decode(uint32_t idx, const Dims& dm, int& x, int& y, int& z) {
-  const uint32_t sl = (uint32_t)dm.w * (uint32_t)dm.h;
-  z = (int)(idx / sl);
-  const uint32_t rem = idx - (uint32_t)z * sl;
-  y = (int)(rem / (uint32_t)dm.w);
-  x = (int)(rem - (uint32_t)y * (uint32_t)dm.w);
-}
 
 // One thread per ridge: every tile whose box the ball reaches (closest point of
 // the tile within r^2 of the centre).  COUNT: counts[bin]++; else: place the
@@ -145,7 +138,7 @@ __device__ __forceinline__ void decode(uint32_t idx, const Dims& dm, int& x, int
 template <bool COUNT>
 __global__ void __launch_bounds__(256)
 bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, const uint32_t* __restrict__ rank_desc,
-           FillInfo* info, Dims dm, Geom g, uint32_t* __restrict__ counts,
+           FillInfo* info, Dims dm, VoxelDecoder vd, Geom g, uint32_t* __restrict__ counts,
            const uint32_t* __restrict__ offsets, uint32_t* __restrict__ entries) {
   const unsigned long long nr = ctr->ridges;
   const uint32_t nR = info->nR;
@@ -155,7 +148,7 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
     const uint2 rec = ridges[i];
     const uint32_t R = rec.y;
     int x, y, z;
-    decode(rec.x, dm, x, y, z);
+    vd(rec.x, x, y, z);
     const int rad = (int)csqrt_u32(R);
     const uint32_t rank = rank_desc[R];
     const int tx0 = max(x - rad, 0) / kFillTX, tx1 = min(x + rad, dm.w - 1) / kFillTX;
@@ -199,13 +192,6 @@ constexpr int kRows = kFillTZ * kFillTY;  // 512 rows of 32 voxels per tile
 
 __device__ __forceinline__ uint32_t range_mask(int a, int b) {  // bits a..b, 0 <= a <= b <= 31
   return (0xffffffffu >> (31 - b)) & (0xffffffffu << a);
-}
-
-// Selection word of row (z, y), word c of a row-padded bitmask; 0 outside the volume.
-__device__ __forceinline__ uint32_t sel_word(const uint32_t* __restrict__ selbits, const Dims& dm, int nw, int z, int y,
-                                             int c) {
-  if (z < 0 || z >= dm.d || y < 0 || y >= dm.h || c < 0 || c >= nw) return 0u;
-  return selbits[((long long)z * dm.h + y) * nw + c];
 }
 
 constexpr int kBinChunk = 256;    // bins whose offsets are staged in shared memory at a time
@@ -270,7 +256,8 @@ constexpr size_t kTileFillSmemWords = (size_t)kRows * 16 + kRows + (kBinChunk + 
 __global__ void __launch_bounds__(kFillThreads, 4)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
                  const uint32_t* __restrict__ rvals, const uint4* __restrict__ rgeo, const FillInfo* __restrict__ info,
-                 const uint32_t* __restrict__ selbits, Dims dm, Geom g, uint32_t* __restrict__ fillmap) {
+                 const uint32_t* __restrict__ selbits, Dims dm, VoxelDecoder vd, Geom g,
+                 uint32_t* __restrict__ fillmap) {
   extern __shared__ uint32_t smem[];
   uint16_t* val = reinterpret_cast<uint16_t*>(smem);       // kRows * 32 half-words
   uint32_t* usel = smem + kRows * 16;                        // kRows
@@ -382,7 +369,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             const uint32_t lo = ss, hi = min(ss + (uint32_t)kEntWin, off[nR]);
             for (uint32_t i = lo + tid; i < hi; i += kFillThreads) {
               int cx, cy, cz;
-              decode(entries[i], dm, cx, cy, cz);
+              vd(entries[i], cx, cy, cz);
               ent[i - lo] = (uint32_t)(cx - x0 + 512) | ((uint32_t)(cy - y0 + 512) << 10) |
                             ((uint32_t)(cz - z0 + 512) << 20);
             }
@@ -504,7 +491,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
 // leaves every non-selected voxel at 0.
 __global__ void __launch_bounds__(256)
 site_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, const uint32_t* __restrict__ selbits,
-            const uint32_t* __restrict__ surf_off, const uint32_t* __restrict__ surf_pts, Dims dm,
+            const uint32_t* __restrict__ surf_off, const uint32_t* __restrict__ surf_pts, Dims dm, VoxelDecoder vd,
             uint32_t* __restrict__ fillmap) {
   const unsigned long long nr = ctr->ridges;
   const int hl = threadIdx.x & 15;
@@ -515,7 +502,7 @@ site_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, 
     const uint2 rec = ridges[i];
     const uint32_t R = rec.y;
     int x, y, z;
-    decode(rec.x, dm, x, y, z);
+    vd(rec.x, x, y, z);
     const uint32_t p1 = surf_off[R + 1];
     for (uint32_t p = surf_off[R] + hl; p < p1; p += 16) {
       const uint32_t pk = surf_pts[p];
@@ -646,9 +633,11 @@ cudaError_t launch_bin(bool count, const uint2* ridges, const Counters* ctr, uns
   const Geom g = geom_of(dm);
   const unsigned blocks = blocks_for((long long)max_ridges, 256, 152 * 32);
   if (count)
-    bin_kernel<true><<<blocks, 256, 0, s>>>(ridges, ctr, rank_desc, info, dm, g, counts, offsets, entries);
+    bin_kernel<true><<<blocks, 256, 0, s>>>(ridges, ctr, rank_desc, info, dm, VoxelDecoder::of(dm), g, counts,
+                                            offsets, entries);
   else
-    bin_kernel<false><<<blocks, 256, 0, s>>>(ridges, ctr, rank_desc, info, dm, g, counts, offsets, entries);
+    bin_kernel<false><<<blocks, 256, 0, s>>>(ridges, ctr, rank_desc, info, dm, VoxelDecoder::of(dm), g, counts,
+                                             offsets, entries);
   ++*launches;
   return cudaGetLastError();
 }
@@ -673,8 +662,8 @@ cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, c
   cudaError_t e = cudaFuncSetAttribute(tile_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const long long grid = g.ntiles < (1LL << 31) - 1 ? g.ntiles : (1LL << 31) - 1;
-  tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, rgeo, info, selbits, dm, g,
-                                                               fillmap);
+  tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, rgeo, info, selbits, dm,
+                                                               VoxelDecoder::of(dm), g, fillmap);
   ++*launches;
   return cudaGetLastError();
 }
@@ -683,7 +672,7 @@ cudaError_t launch_sites(const uint2* ridges, const Counters* ctr, unsigned long
                          const uint32_t* selbits, const uint32_t* surf_off, const uint32_t* surf_pts, Dims dm,
                          uint32_t* fillmap, cudaStream_t s, unsigned long long* launches) {
   const unsigned blocks = blocks_for((long long)max_ridges, 16, 152 * 16);
-  site_kernel<<<blocks, 256, 0, s>>>(ridges, ctr, selbits, surf_off, surf_pts, dm, fillmap);
+  site_kernel<<<blocks, 256, 0, s>>>(ridges, ctr, selbits, surf_off, surf_pts, dm, VoxelDecoder::of(dm), fillmap);
   ++*launches;
   return cudaGetLastError();
 }
