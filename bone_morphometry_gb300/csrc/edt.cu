@@ -10,6 +10,9 @@
 //   pass y, z : lower envelope of the parabolas (q - p)^2 + f(p) with the
 //            intersection test done by int64 cross-multiplication; lines
 //            whose every entry is "no site" (kInfSq) stay kInfSq.
+#include <cuda.h>  // CUtensorMap and its enums (types only; the encoder comes from the runtime)
+#include <cudaTypedefs.h>
+
 #include <climits>
 #include <cstdint>
 
@@ -29,9 +32,113 @@ __device__ __forceinline__ bool selected_at(const uint8_t* __restrict__ a, const
 }
 
 constexpr int kXWarps = 8;
+constexpr int kNoLeft = -(1 << 20);  // sentinels: no site on that side (w <= 32768)
+constexpr int kNoRight = 1 << 21;
+
+// Second half of the x pass for one row whose site bitmask (1 = non-selected
+// voxel) is in mask[0 .. nw): two warp scans give lastpos[c], the highest
+// site position in words <= c, and firstpos[c], the lowest in words >= c, so
+// that every voxel finds its nearest site on each side without branching:
+// inside its own word from the bits below / above it, else from the neighbour
+// word's entry.
+__device__ __forceinline__ void x_row_scans(const uint32_t* mask, int* lastpos, int* firstpos, int nw, int lane) {
+  int carry = kNoLeft;
+  for (int c0 = 0; c0 < nw; c0 += 32) {
+    const int c = c0 + lane;
+    const uint32_t m = c < nw ? mask[c] : 0u;
+    int v = m ? c * 32 + 31 - __clz(m) : kNoLeft;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v = max(v, t);
+    }
+    v = max(v, carry);
+    if (c < nw) lastpos[c] = v;
+    carry = __shfl_sync(0xffffffffu, v, 31);
+  }
+  carry = kNoRight;
+  for (int c0 = ((nw - 1) >> 5) << 5; c0 >= 0; c0 -= 32) {
+    const int c = c0 + lane;
+    const uint32_t m = c < nw ? mask[c] : 0u;
+    int v = m ? c * 32 + __ffs(m) - 1 : kNoRight;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_down_sync(0xffffffffu, v, o);
+      if (lane + o < 32) v = min(v, t);
+    }
+    v = min(v, carry);
+    if (c < nw) firstpos[c] = v;
+    carry = __shfl_sync(0xffffffffu, v, 0);
+  }
+  __syncwarp();
+}
+
+// Squared distance of voxel x to the nearer of its sites left / right
+// (kInfSq when neither exists; 0 when x is a site).
+__device__ __forceinline__ uint32_t x_dist(bool site, int x, int left, int right) {
+  const int g = min(x - left, right - x);
+  return site ? 0u : (g >= (1 << 20) ? kInfSq : (uint32_t)g * (uint32_t)g);
+}
+
+// One voxel per lane per word: one coalesced 128-byte store per word.
+__device__ __forceinline__ void x_row_distances(const uint32_t* mask, int* lastpos, int* firstpos, int nw, int w,
+                                                int lane, uint32_t* __restrict__ orow) {
+  x_row_scans(mask, lastpos, firstpos, nw, lane);
+  const uint32_t below = (1u << lane) - 1u, above = ~((2u << lane) - 1u);  // lane 31: above = 0
+#pragma unroll 1
+  for (int c = 0; c < nw; ++c) {
+    const int x = c * 32 + lane;
+    const uint32_t m = mask[c];
+    const int lprev = c > 0 ? lastpos[c - 1] : kNoLeft;
+    const int rnext = c + 1 < nw ? firstpos[c + 1] : kNoRight;
+    const uint32_t lo = m & below, hi = m & above;
+    const int left = lo ? c * 32 + 31 - __clz(lo) : lprev;
+    const int right = hi ? c * 32 + __ffs(hi) - 1 : rnext;
+    if (x < w) orow[x] = x_dist((m >> lane) & 1u, x, left, right);
+  }
+  __syncwarp();
+}
+
+// Four adjacent voxels per lane (rows whose length is a multiple of 16 and
+// whose start is 16-byte aligned): the nearest site left of the first voxel
+// and right of the last come from the word and scan entries as above, the
+// others follow from the three bits between them; one 16-byte store per lane,
+// 512 bytes per warp.
+__device__ __forceinline__ void x_row_distances4(const uint32_t* mask, int* lastpos, int* firstpos, int nw, int w,
+                                                 int lane, uint32_t* __restrict__ orow) {
+  x_row_scans(mask, lastpos, firstpos, nw, lane);
+  const int b = (lane & 7) * 4;  // first bit of this lane's voxels in their word
+  const uint32_t below = (1u << b) - 1u, above = ~((2u << (b + 3)) - 1u);  // b + 3 = 31: above = 0
+#pragma unroll 1
+  for (int x0 = 0; x0 < w; x0 += 128) {
+    const int x = x0 + 4 * lane;
+    if (x < w) {
+      const int c = x >> 5;
+      const uint32_t m = mask[c];
+      const int cb = c * 32 + b;
+      const uint32_t lo = m & below, hi = m & above;
+      const int l0 = lo ? c * 32 + 31 - __clz(lo) : (c > 0 ? lastpos[c - 1] : kNoLeft);
+      const int r3 = hi ? c * 32 + __ffs(hi) - 1 : (c + 1 < nw ? firstpos[c + 1] : kNoRight);
+      const uint32_t bits = m >> b;  // this lane's 4 voxels in bits 0..3
+      const int l1 = (bits & 1u) ? cb : l0;
+      const int l2 = (bits & 2u) ? cb + 1 : l1;
+      const int l3 = (bits & 4u) ? cb + 2 : l2;
+      const int r2 = (bits & 8u) ? cb + 3 : r3;
+      const int r1 = (bits & 4u) ? cb + 2 : r2;
+      const int r0 = (bits & 2u) ? cb + 1 : r1;
+      uint4 v;
+      v.x = x_dist(bits & 1u, x, l0, r0);
+      v.y = x_dist(bits & 2u, x + 1, l1, r1);
+      v.z = x_dist(bits & 4u, x + 2, l2, r2);
+      v.w = x_dist(bits & 8u, x + 3, l3, r3);
+      *reinterpret_cast<uint4*>(orow + x) = v;
+    }
+  }
+  __syncwarp();
+}
 
 // One warp per x row.  Shared memory per warp: site bitmask of the row and, per
-// word, the nearest non-empty word at-or-before / at-or-after it.
+// word, the nearest site position at-or-before / at-or-after it.
 template <int MODE>
 __global__ void __launch_bounds__(kXWarps * 32)
 edt_x_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, Dims dm, uint32_t* __restrict__ out,
@@ -41,8 +148,8 @@ edt_x_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, Dims 
   const int warp = threadIdx.x >> 5;
   const int nw = dm.nw();
   uint32_t* mask = smem + (size_t)warp * 3 * nw;
-  int* prevnz = reinterpret_cast<int*>(mask + nw);
-  int* nextnz = prevnz + nw;
+  int* lastpos = reinterpret_cast<int*>(mask + nw);
+  int* firstpos = lastpos + nw;
   const long long rows = (long long)dm.h * dm.d;
   unsigned long long sites = 0;
 
@@ -62,63 +169,7 @@ edt_x_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, Dims 
       }
     }
     __syncwarp();
-    int carry = -1;
-    for (int c0 = 0; c0 < nw; c0 += 32) {
-      const int c = c0 + lane;
-      int v = (c < nw && mask[c] != 0u) ? c : -1;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v = max(v, t);
-      }
-      v = max(v, carry);
-      if (c < nw) prevnz[c] = v;
-      carry = __shfl_sync(0xffffffffu, v, 31);
-    }
-    carry = INT_MAX;
-    for (int c0 = ((nw - 1) >> 5) << 5; c0 >= 0; c0 -= 32) {
-      const int c = c0 + lane;
-      int v = (c < nw && mask[c] != 0u) ? c : INT_MAX;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_down_sync(0xffffffffu, v, o);
-        if (lane + o < 32) v = min(v, t);
-      }
-      v = min(v, carry);
-      if (c < nw) nextnz[c] = v;
-      carry = __shfl_sync(0xffffffffu, v, 0);
-    }
-    __syncwarp();
-    for (int c = 0; c < nw; ++c) {
-      const int x = c * 32 + lane;
-      if (x < dm.w) {
-        const uint32_t m = mask[c];
-        uint32_t val = 0;
-        if (!((m >> lane) & 1u)) {
-          int left = -1, right = -1;
-          const uint32_t lo = m & ((1u << lane) - 1u);
-          if (lo) {
-            left = c * 32 + 31 - __clz(lo);
-          } else if (c > 0) {
-            const int p = prevnz[c - 1];
-            if (p >= 0) left = p * 32 + 31 - __clz(mask[p]);
-          }
-          const uint32_t hi = (lane == 31) ? 0u : (m & ~((2u << lane) - 1u));
-          if (hi) {
-            right = c * 32 + __ffs(hi) - 1;
-          } else if (c + 1 < nw) {
-            const int p = nextnz[c + 1];
-            if (p != INT_MAX) right = p * 32 + __ffs(mask[p]) - 1;
-          }
-          int g = INT_MAX;
-          if (left >= 0) g = x - left;
-          if (right >= 0) g = min(g, right - x);
-          val = (g == INT_MAX) ? kInfSq : (uint32_t)g * (uint32_t)g;
-        }
-        out[base + x] = val;
-      }
-    }
-    __syncwarp();
+    x_row_distances(mask, lastpos, firstpos, nw, dm.w, lane, out + base);
   }
   if (lane == 0 && sites) atomicAdd(&ctr->sites, sites);
 }
@@ -140,9 +191,9 @@ __device__ __forceinline__ uint32_t sel4(uint32_t a, uint32_t b) {
 // The x pass for rows whose bytes are 16-byte aligned (w a multiple of 16 and
 // aligned inputs): each lane loads 16 voxels of bone and roi at once and the
 // lanes' 16-bit masks pair up into the row's 32-bit words; the distances are
-// then computed as in edt_x_kernel, one x per lane (coalesced stores).
+// then computed four adjacent voxels per lane (16-byte stores).
 template <int MODE>
-__global__ void __launch_bounds__(kXWarps * 32)
+__global__ void __launch_bounds__(kXWarps * 32, 5)
 edt_x_vec_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, Dims dm, uint32_t* __restrict__ out,
                  uint32_t* __restrict__ selbits, Counters* __restrict__ ctr) {
   extern __shared__ uint32_t smem[];
@@ -150,8 +201,8 @@ edt_x_vec_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, D
   const int warp = threadIdx.x >> 5;
   const int nw = dm.nw();
   uint32_t* mask = smem + (size_t)warp * 3 * nw;
-  int* prevnz = reinterpret_cast<int*>(mask + nw);
-  int* nextnz = prevnz + nw;
+  int* lastpos = reinterpret_cast<int*>(mask + nw);
+  int* firstpos = lastpos + nw;
   const long long rows = (long long)dm.h * dm.d;
   const bool two = MODE == SEL_BONE_IN_ROI || MODE == SEL_MARROW_IN_ROI;
   unsigned long long sites = 0;
@@ -186,63 +237,7 @@ edt_x_vec_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b, D
       }
     }
     __syncwarp();
-    int carry = -1;
-    for (int c0 = 0; c0 < nw; c0 += 32) {
-      const int c = c0 + lane;
-      int v = (c < nw && mask[c] != 0u) ? c : -1;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v = max(v, t);
-      }
-      v = max(v, carry);
-      if (c < nw) prevnz[c] = v;
-      carry = __shfl_sync(0xffffffffu, v, 31);
-    }
-    carry = INT_MAX;
-    for (int c0 = ((nw - 1) >> 5) << 5; c0 >= 0; c0 -= 32) {
-      const int c = c0 + lane;
-      int v = (c < nw && mask[c] != 0u) ? c : INT_MAX;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_down_sync(0xffffffffu, v, o);
-        if (lane + o < 32) v = min(v, t);
-      }
-      v = min(v, carry);
-      if (c < nw) nextnz[c] = v;
-      carry = __shfl_sync(0xffffffffu, v, 0);
-    }
-    __syncwarp();
-    for (int c = 0; c < nw; ++c) {
-      const int x = c * 32 + lane;
-      if (x < dm.w) {
-        const uint32_t m = mask[c];
-        uint32_t val = 0;
-        if (!((m >> lane) & 1u)) {
-          int left = -1, right = -1;
-          const uint32_t lo = m & ((1u << lane) - 1u);
-          if (lo) {
-            left = c * 32 + 31 - __clz(lo);
-          } else if (c > 0) {
-            const int p = prevnz[c - 1];
-            if (p >= 0) left = p * 32 + 31 - __clz(mask[p]);
-          }
-          const uint32_t hi = (lane == 31) ? 0u : (m & ~((2u << lane) - 1u));
-          if (hi) {
-            right = c * 32 + __ffs(hi) - 1;
-          } else if (c + 1 < nw) {
-            const int p = nextnz[c + 1];
-            if (p != INT_MAX) right = p * 32 + __ffs(mask[p]) - 1;
-          }
-          int g = INT_MAX;
-          if (left >= 0) g = x - left;
-          if (right >= 0) g = min(g, right - x);
-          val = (g == INT_MAX) ? kInfSq : (uint32_t)g * (uint32_t)g;
-        }
-        out[base + x] = val;
-      }
-    }
-    __syncwarp();
+    x_row_distances4(mask, lastpos, firstpos, nw, dm.w, lane, out + base);
   }
   if (lane == 0 && sites) atomicAdd(&ctr->sites, sites);
 }
@@ -328,21 +323,36 @@ edt_line_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int
 // A CTA owns 32 consecutive x of one line-row and kWinTL consecutive outputs
 // along the axis; it stages those inputs in shared memory as 128-byte rows,
 // then a halo on each side as wide as the largest window it needs (at most
-// kWinHalo).  Each lane scans outwards from its output and stops once dp^2
-// reaches the best value found.  Lines with an output whose window exceeds the
-// halo (or that has no site at all, f = kInfSq) are marked in `redo`; the
+// kWinHalo).  Each lane computes four adjacent outputs q .. q+3 of its column
+// at once: the loads at q - e and q + 3 + e serve all four (at distances
+// k + e and 3 - k + e for output q + k), so a scan step costs two shared loads
+// for four outputs.  The scan runs outwards until e^2 reaches the largest of
+// the four minima.  Lines with an output whose window exceeds the halo (or
+// that have no site at all, f = kInfSq) are marked in `redo`; the
 // lower-envelope kernel recomputes exactly those lines afterwards.
 constexpr int kWinTL = 128;
 constexpr int kWinHalo = 64;
 constexpr int kWinThreads = 256;
 constexpr int kWinWarps = kWinThreads / 32;
-static_assert(kInfSq + (kWinHalo + 3u) * (kWinHalo + 3u) > kInfSq, "the window scan adds dp^2 to kInfSq");
+constexpr int kWinGroup = 4;  // adjacent outputs per lane
+static_assert(kWinTL == kWinWarps * kWinGroup * 4, "four groups of four outputs per warp");
+static_assert(kInfSq + (kWinHalo + 6u) * (kWinHalo + 6u) > kInfSq, "the window scan adds distance^2 to kInfSq");
 
 // floor(sqrt(f)) + 2 >= isqrt(f - 1) + 1 for f >= 1: the halo that f needs,
 // from the hardware reciprocal square root (error far below one).
 __device__ __forceinline__ uint32_t halo_need(uint32_t f) {
   const float ff = (float)f;
   return (uint32_t)(ff * rsqrtf(ff)) + 2u;
+}
+
+// One scan step at offset e: left candidate L = f(q - e), right R = f(q + 3 + e).
+__device__ __forceinline__ void win_step(uint32_t L, uint32_t R, uint32_t e, uint32_t& b0, uint32_t& b1,
+                                         uint32_t& b2, uint32_t& b3) {
+  const uint32_t s0 = e * e, s1 = s0 + 2u * e + 1u, s2 = s1 + 2u * e + 3u, s3 = s2 + 2u * e + 5u;
+  b0 = __viaddmin_u32(L, s0, __viaddmin_u32(R, s3, b0));
+  b1 = __viaddmin_u32(L, s1, __viaddmin_u32(R, s2, b1));
+  b2 = __viaddmin_u32(L, s2, __viaddmin_u32(R, s1, b2));
+  b3 = __viaddmin_u32(L, s3, __viaddmin_u32(R, s0, b3));
 }
 
 __global__ void __launch_bounds__(kWinThreads)
@@ -399,49 +409,192 @@ edt_window_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, i
   __syncthreads();
   uint32_t localmax = 0;
   bool bad = false;
-  uint32_t* op = out + base + (long long)(q0 + warp) * stride;  // output of row j, advanced per j
-  const long long ostep = (long long)kWinWarps * stride;
 #pragma unroll 1
-  for (int j = 0; j < kPer; ++j, op += ostep) {
-    const int i = warp + kWinWarps * j;
+  for (int j = 0; j < kPer / kWinGroup; ++j) {
+    const int i = kWinGroup * (warp + kWinWarps * j);  // first of the group's rows (warp-uniform)
     const int q = q0 + i;
     if (!xin || q >= n) continue;
+    const int m = min(kWinGroup, n - q);  // outputs inside the line
     const uint32_t* col = buf + (kWinHalo + i) * 32 + lane;
-    uint32_t best = col[0];
-    if (best == 0u) {
-      *op = 0u;
-      continue;
+    const uint32_t c0 = col[0], c1 = col[32], c2 = col[64], c3 = col[96];
+    // the group's own values (rows past the line end hold kInfSq)
+    uint32_t b0 = __viaddmin_u32(c1, 1u, __viaddmin_u32(c2, 4u, __viaddmin_u32(c3, 9u, c0)));
+    uint32_t b1 = __viaddmin_u32(c0, 1u, __viaddmin_u32(c2, 1u, __viaddmin_u32(c3, 4u, c1)));
+    uint32_t b2 = __viaddmin_u32(c0, 4u, __viaddmin_u32(c1, 1u, __viaddmin_u32(c3, 1u, c2)));
+    uint32_t b3 = __viaddmin_u32(c0, 9u, __viaddmin_u32(c1, 4u, __viaddmin_u32(c2, 1u, c3)));
+    if (m < 4) {  // outputs past the line end take no part in the stopping test
+      b3 = 0u;
+      if (m < 3) b2 = 0u;
+      if (m < 2) b1 = 0u;
     }
-    // every p with |q - p| < dp has been tried once dp^2 >= best (a step
-    // with dp^2 >= best cannot lower it, so four steps run at a time); if the
-    // scan would have to pass the staged halo, the line is redone exactly
+    // after offsets 1 .. e-1 every candidate within distance e of every output
+    // has been tried, so the scan stops once e^2 reaches the largest minimum
     bool done = true;
-    int dp = 1;
-    while ((uint32_t)(dp * dp) < best) {
-      if (dp + 3 <= halo) {
+    int e = 1;
+    uint32_t mx = max(max(b0, b1), max(b2, b3));
+    while ((uint32_t)(e * e) < mx) {
+      if (e + 3 <= halo) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int d = dp + u;
-          best = min(best, min(col[-d * 32], col[d * 32]) + (uint32_t)(d * d));
-        }
-        dp += 4;
+        for (int u = 0; u < 4; ++u)
+          win_step(col[-(e + u) * 32], col[(3 + e + u) * 32], (uint32_t)(e + u), b0, b1, b2, b3);
+        e += 4;
       } else {
-        if (dp > halo) {
+        if (e > halo) {
           done = false;
           break;
         }
-        best = min(best, min(col[-dp * 32], col[dp * 32]) + (uint32_t)(dp * dp));
-        ++dp;
+        win_step(col[-e * 32], col[(3 + e) * 32], (uint32_t)e, b0, b1, b2, b3);
+        ++e;
       }
+      mx = max(max(b0, b1), max(b2, b3));
     }
     if (!done) {
       bad = true;
       continue;
     }
-    *op = best;
-    localmax = max(localmax, best);
+    uint32_t* op = out + base + (long long)q * stride;
+    op[0] = b0;
+    if (m > 1) op[stride] = b1;
+    if (m > 2) op[2 * stride] = b2;
+    if (m > 3) op[3 * stride] = b3;
+    localmax = max(localmax, mx);
   }
   if (bad) redo[orow * (long long)w + x] = 1u;
+  if (track_max) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) localmax = max(localmax, __shfl_xor_sync(0xffffffffu, localmax, o));
+    if (lane == 0 && localmax) atomicMax(&ctr->rmax, localmax);
+  }
+}
+
+
+// ---- TMA-staged window pass -------------------------------------------------
+// Same computation as edt_window_kernel, with the staging done by the tensor
+// memory accelerator: one thread issues a single 3-D tiled copy of the block's
+// 128 output rows plus a full 64-row halo on each side (256 rows of 32 x,
+// 32 KB) into shared memory and every thread waits on the copy's mbarrier.
+// Rows outside the line arrive zero-filled and are set to kInfSq ("no site")
+// by the blocks at the line ends.  The per-thread load, staging and halo
+// sizing work of the plain kernel disappears; the scan may always run to the
+// full halo.  Needs w a multiple of 4 (16-byte row pitch) and 16-byte aligned
+// buffers; other volumes, and the z pass, take edt_window_kernel.
+constexpr int kTmaRows = kWinTL + 2 * kWinHalo;
+static_assert(kTmaRows <= 256, "a TMA box dimension is at most 256");
+constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz: a copy that has not landed by then never will
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Bounded wait for phase `parity` of the mbarrier at `bar`.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+}
+
+__global__ void __launch_bounds__(kWinThreads)
+edt_window_tma_kernel(const __grid_constant__ CUtensorMap tin, uint32_t* __restrict__ out, int axis, int n,
+                      long long stride, int w, long long outer_stride, int nxt, int nchunk,
+                      uint8_t* __restrict__ redo, Counters* __restrict__ ctr, int track_max) {
+  __shared__ alignas(128) uint32_t buf[kTmaRows * 32];
+  __shared__ alignas(8) unsigned long long bar;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long bid = blockIdx.x;
+  const int xt = (int)(bid % nxt);
+  const int chunk = (int)((bid / nxt) % nchunk);
+  const int orow = (int)(bid / ((long long)nxt * nchunk));
+  const int x = xt * 32 + lane;
+  const bool xin = x < w;
+  const int q0 = chunk * kWinTL;
+  const uint32_t b = smem_u32(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int c0 = xt * 32, ql = q0 - kWinHalo;  // x start: 128-byte multiple; rows may start below 0
+    const int c1 = axis == 1 ? ql : orow, c2 = axis == 1 ? orow : ql;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(kTmaRows * 32 * 4)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(buf)), "l"(reinterpret_cast<unsigned long long>(&tin)), "r"(c0), "r"(c1), "r"(c2), "r"(b)
+        : "memory");
+  }
+  const bool landed = mbar_wait(b, 0u);
+  if (!__syncthreads_and(landed)) {
+    // the copy did not complete: report it, give the copy in flight a second
+    // bounded wait (it writes into this block's shared memory) and leave
+    if (threadIdx.x == 0) atomicOr(&ctr->status, 1u);
+    mbar_wait(b, 0u);
+    return;
+  }
+  if (q0 < kWinHalo || q0 + kWinTL + kWinHalo > n) {
+    for (int k = threadIdx.x; k < kTmaRows * 32; k += kWinThreads) {
+      const int q = q0 - kWinHalo + (k >> 5);
+      if (q < 0 || q >= n) buf[k] = kInfSq;
+    }
+    __syncthreads();
+  }
+  const long long base = (long long)orow * outer_stride + x;
+  uint32_t localmax = 0;
+  bool bad = false;
+#pragma unroll 1
+  for (int j = 0; j < kWinTL / (kWinGroup * kWinWarps); ++j) {
+    const int i = kWinGroup * (warp + kWinWarps * j);
+    const int q = q0 + i;
+    if (!xin || q >= n) continue;
+    const int m = min(kWinGroup, n - q);
+    const uint32_t* col = buf + (kWinHalo + i) * 32 + lane;
+    const uint32_t c0 = col[0], c1 = col[32], c2 = col[64], c3 = col[96];
+    uint32_t b0 = __viaddmin_u32(c1, 1u, __viaddmin_u32(c2, 4u, __viaddmin_u32(c3, 9u, c0)));
+    uint32_t b1 = __viaddmin_u32(c0, 1u, __viaddmin_u32(c2, 1u, __viaddmin_u32(c3, 4u, c1)));
+    uint32_t b2 = __viaddmin_u32(c0, 4u, __viaddmin_u32(c1, 1u, __viaddmin_u32(c3, 1u, c2)));
+    uint32_t b3 = __viaddmin_u32(c0, 9u, __viaddmin_u32(c1, 4u, __viaddmin_u32(c2, 1u, c3)));
+    if (m < 4) {
+      b3 = 0u;
+      if (m < 3) b2 = 0u;
+      if (m < 2) b1 = 0u;
+    }
+    bool done = true;
+    int e = 1;
+    uint32_t mx = max(max(b0, b1), max(b2, b3));
+    while ((uint32_t)(e * e) < mx) {
+      if (e + 3 <= kWinHalo) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          win_step(col[-(e + u) * 32], col[(3 + e + u) * 32], (uint32_t)(e + u), b0, b1, b2, b3);
+        e += 4;
+      } else {
+        if (e > kWinHalo) {
+          done = false;
+          break;
+        }
+        win_step(col[-e * 32], col[(3 + e) * 32], (uint32_t)e, b0, b1, b2, b3);
+        ++e;
+      }
+      mx = max(max(b0, b1), max(b2, b3));
+    }
+    if (!done) {
+      bad = true;
+      continue;
+    }
+    uint32_t* op = out + base + (long long)q * stride;
+    op[0] = b0;
+    if (m > 1) op[stride] = b1;
+    if (m > 2) op[2 * stride] = b2;
+    if (m > 3) op[3 * stride] = b3;
+    localmax = max(localmax, mx);
+  }
+  if (bad) redo[(long long)orow * w + x] = 1u;
   if (track_max) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) localmax = max(localmax, __shfl_xor_sync(0xffffffffu, localmax, o));
@@ -462,7 +615,8 @@ cudaError_t launch_edt_x_mode(const uint8_t* a, const uint8_t* b, Dims dm, uint3
                               Counters* ctr, unsigned blocks, size_t smem, cudaStream_t s) {
   const bool two = MODE == SEL_BONE_IN_ROI || MODE == SEL_MARROW_IN_ROI;
   const bool vec = dm.w % 16 == 0 && (reinterpret_cast<uintptr_t>(a) & 15u) == 0 &&
-                   (!two || (reinterpret_cast<uintptr_t>(b) & 15u) == 0);
+                   (!two || (reinterpret_cast<uintptr_t>(b) & 15u) == 0) &&
+                   (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
   if (vec) {
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(edt_x_vec_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -528,6 +682,37 @@ cudaError_t launch_edt_line(int axis, const uint32_t* in, uint32_t* out, Dims dm
   return cudaGetLastError();
 }
 
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of a u32 volume (x fastest) whose box is 32 x by `rows` along the
+// pass axis; false when the volume or buffer does not meet TMA's rules.
+bool window_map(CUtensorMap* map, const uint32_t* vol, Dims dm, int axis, unsigned rows) {
+  if (dm.w % 4 != 0 || (reinterpret_cast<uintptr_t>(vol) & 15u) != 0) return false;
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)dm.w, (cuuint64_t)dm.h, (cuuint64_t)dm.d};
+  const cuuint64_t pitch[2] = {(cuuint64_t)dm.w * 4, (cuuint64_t)dm.w * dm.h * 4};
+  const cuuint32_t box[3] = {32u, axis == 1 ? rows : 1u, axis == 1 ? 1u : rows};
+  const cuuint32_t unit[3] = {1u, 1u, 1u};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint32_t*>(vol), dims, pitch, box, unit,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
 cudaError_t launch_edt_window(int axis, const uint32_t* in, uint32_t* out, Dims dm, void* scratch, uint8_t* redo,
                               Counters* ctr, cudaStream_t s, unsigned long long* launches) {
   int n;
@@ -550,8 +735,18 @@ cudaError_t launch_edt_window(int axis, const uint32_t* in, uint32_t* out, Dims 
   const int nxt = (dm.w + 31) / 32;
   const int nchunk = (n + kWinTL - 1) / kWinTL;
   const long long blocks = (long long)nxt * nchunk * orows;
-  edt_window_kernel<<<(unsigned)blocks, kWinThreads, 0, s>>>(in, out, n, stride, dm.w, outer, nxt, nchunk, redo, ctr,
-                                                             axis == 2 ? 1 : 0);
+  // TMA staging for the y pass only: a z-pass box spans 256 rows a whole
+  // slice apart (a different page each), which the copy engine translates one
+  // by one; there the per-thread loads measured faster (2.2 against 3.0 ms on
+  // 1024^3 bone).
+  CUtensorMap map;
+  if (axis == 1 && window_map(&map, in, dm, axis, kTmaRows)) {
+    edt_window_tma_kernel<<<(unsigned)blocks, kWinThreads, 0, s>>>(map, out, axis, n, stride, dm.w, outer, nxt,
+                                                                   nchunk, redo, ctr, axis == 2 ? 1 : 0);
+  } else {
+    edt_window_kernel<<<(unsigned)blocks, kWinThreads, 0, s>>>(in, out, n, stride, dm.w, outer, nxt, nchunk, redo,
+                                                               ctr, axis == 2 ? 1 : 0);
+  }
   ++*launches;
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -216,6 +216,45 @@ def test_device_tensor_path(gpu_ctx):
     assert np.array_equal(e, O.edt_sq(vol.cpu().numpy()))
 
 
+def test_device_inputs_at_odd_offsets(gpu_ctx):
+    """Bone and ROI tensors that start off a 16-byte boundary (byte-loop count
+    and scalar x pass) give the same results as aligned ones."""
+    import torch
+
+    sp = S.make_specimen((18, 26, 64), 2.0, 0.3, "cylinder", 11.0, 9.0, 81)
+    n = sp.bone.size
+    ref = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx)
+    for ob, orr in ((1, 3), (0, 5), (7, 0)):
+        bb = torch.zeros(n + 16, dtype=torch.uint8, device="cuda")
+        rb = torch.zeros(n + 16, dtype=torch.uint8, device="cuda")
+        bb[ob:ob + n] = torch.from_numpy(sp.bone.ravel()).cuda()
+        rb[orr:orr + n] = torch.from_numpy(sp.roi.ravel()).cuda()
+        got = analyze_thickness(bb[ob:ob + n].view(sp.bone.shape), rb[orr:orr + n].view(sp.roi.shape),
+                                sp.spacing_um, ctx=gpu_ctx)
+        assert got.thickness.mean == ref.thickness.mean and got.spacing.mean == ref.spacing.mean
+        assert got.spacing.maximum == ref.spacing.maximum
+
+
+@pytest.mark.parametrize("shape", [(4, 4, 4), (3, 5, 7), (6, 9, 37)])
+def test_roi_counts_in_the_tail(gpu_ctx, shape):
+    """The bails see ROI and bone voxels that sit only in the last n % 32 bytes."""
+    n = int(np.prod(shape))
+    bone = np.zeros(shape, np.uint8)
+    roi = np.zeros(shape, np.uint8)
+    with pytest.raises(BoneMorphometryError, match="ROI mask contains no included voxels"):
+        analyze_thickness(bone, roi, 1.0, ctx=gpu_ctx)
+    flat_r = roi.reshape(-1)
+    flat_r[n - 2:] = 1
+    with pytest.raises(BoneMorphometryError, match="ROI contains no bone voxels"):
+        analyze_thickness(bone, roi, 1.0, ctx=gpu_ctx)
+    bone.reshape(-1)[n - 2:] = 255
+    with pytest.raises(BoneMorphometryError, match="ROI contains no marrow voxels"):
+        analyze_thickness(bone, roi, 1.0, ctx=gpu_ctx)
+    bone.reshape(-1)[n - 1] = 0
+    res = analyze_thickness(bone, roi, 1.0, ctx=gpu_ctx)
+    assert res.thickness.mean > 0 and res.spacing.mean > 0
+
+
 def test_phases_side_by_side_or_sequential_agree(gpu_ctx):
     """Tb.Th / Tb.Sp with the two phases on two streams (default) and one after
     the other: identical maps and statistics, quantiles included."""
