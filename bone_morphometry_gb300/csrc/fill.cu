@@ -12,8 +12,8 @@
 // later ball skip whatever is already decided.  Balls of equal r^2 paint the
 // same value and run concurrently; a barrier separates consecutive r^2 groups.
 // Each group is processed in rounds: a plane test per (ball, plane) against a
-// range-OR table of the masks, then a load-balanced pass that paints the
-// chords of the planes that passed, one row per lane.
+// range-OR table of the masks, then a pass that paints the chords of the
+// planes that passed, each plane walked by a group of 1 to 8 threads.
 //
 // Non-selected voxels: a ball reaches one only on its sphere (its r^2 is the
 // distance to the nearest non-selected voxel), so a per-ridge pass over the
@@ -194,6 +194,11 @@ __device__ __forceinline__ uint32_t range_mask(int a, int b) {  // bits a..b, 0 
   return (0xffffffffu >> (31 - b)) & (0xffffffffu << a);
 }
 
+// Word of row (z, y) in the unpainted-voxel masks: rotated by 3z within the
+// plane, so that threads reading the same y of consecutive planes (the planes
+// of one ball) fall into different banks.
+__device__ __forceinline__ int urow(int z, int y) { return z * kFillTY + ((y + 3 * z) & (kFillTY - 1)); }
+
 constexpr int kBinChunk = 256;    // bins whose offsets are staged in shared memory at a time
 constexpr int kEntWin = 768;      // ball entries staged in shared memory at a time
 constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself)
@@ -201,6 +206,7 @@ constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the rang
 constexpr int kRotStride = 33;    // words per range-OR row: lanes testing different planes hit different banks
 constexpr int kItems = 1024;      // (ball, plane) paint items per round
 constexpr int kHxMax = 31;        // balls up to this radius read their chord half-widths from a table
+constexpr int kHxStride = 36;     // bytes per |dz| row of that table (9 words: rows of consecutive planes in different banks)
 constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
 
 // rot[lv - 1][z][y] (rows of kRotStride words) = OR of the unpainted-voxel
@@ -209,7 +215,7 @@ constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields
 __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uint32_t* __restrict__ rot, int warp,
                                           int lane, int nwarps) {
   for (int zz = warp; zz < kFillTZ; zz += nwarps) {
-    uint32_t v = usel[zz * kFillTY + lane];
+    uint32_t v = usel[urow(zz, lane)];
 #pragma unroll
     for (int lv = 1; lv < kRotLevels; ++lv) {
       const uint32_t u = __shfl_down_sync(0xffffffffu, v, 1 << (lv - 1));
@@ -228,7 +234,7 @@ __device__ __forceinline__ int vidx(int row, int x) {
 
 constexpr size_t kTileFillSmemWords = (size_t)kRows * 16 + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
                                       (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130 +
-                                      (kHxMax + 1) * (kHxMax + 1) / 4;
+                                      (kHxMax + 1) * kHxStride / 4;
 
 // One CTA per tile (32 x 32 x 16 voxels) paints the tile's selected voxels.
 // Shared memory:
@@ -248,10 +254,11 @@ constexpr size_t kTileFillSmemWords = (size_t)kRows * 16 + kRows + (kBinChunk + 
 // half tests plane zlo + hl of its ball -- the plane needs work only if some
 // open row in the disk's y-range has an unpainted voxel inside the disk's
 // widest chord (a stale range-OR table is a superset, so it never skips work)
-// -- and appends the planes that pass to the item list.  Paint: the warps
-// share the items evenly; for an item all 32 lanes take one row each and
-// paint the chord's unpainted voxels.  Balls of one bin have the same r^2, so
-// the order of their items does not matter.  Non-selected voxels are left 0
+// -- and appends the planes that pass to the item list.  Paint: a group of
+// 1 to 8 threads per item (more when the round has few items) walks the
+// disk's rows and paints each row's chord of unpainted voxels.  Balls of one
+// bin have the same r^2, so the order of their items does not matter (two
+// threads may write the same tag).  Non-selected voxels are left 0
 // here; the site pass adds the ones a sphere reaches.
 __global__ void __launch_bounds__(kFillThreads, 4)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
@@ -267,7 +274,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
   uint32_t* rot = ent + kEntWin;                             // (kRotLevels - 1) * kFillTZ * kRotStride
   uint32_t* item = rot + (kRotLevels - 1) * kFillTZ * kRotStride;  // kItems
   uint16_t* hyt = reinterpret_cast<uint16_t*>(item + kItems);              // 257 (+1) half-words
-  uint8_t* hxt = reinterpret_cast<uint8_t*>(item + kItems + 130);         // (kHxMax + 1)^2 bytes
+  uint8_t* hxt = reinterpret_cast<uint8_t*>(item + kItems + 130);         // (kHxMax + 1) * kHxStride bytes
   __shared__ uint32_t s_nnz, s_wlo, s_whi;
   __shared__ uint32_t s_nitem[2];
   __shared__ uint32_t wcnt[kFillWarps];
@@ -307,7 +314,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       const int zz = r / kFillTY, yy = r % kFillTY;
       uint32_t own = 0u;
       if (zz < vz && yy < vy) own = selbits[((long long)(z0 + zz) * dm.h + (y0 + yy)) * nw + tx] & xmask;
-      usel[r] = own;
+      usel[urow(zz, yy)] = own;
       any_sel = any_sel || own != 0u;
     }
     if (!__syncthreads_or(any_sel)) {  // nothing selected here (outside the ROI, say): all zero
@@ -352,13 +359,13 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
         const int rad = (int)gq.z;                         // isqrt(r2): no lattice point of the ball is further
         const uint32_t e = boff[bl + 1];
         // this bin's disk radii: hyt[|dz|] = isqrt(r2 - dz^2); for small balls
-        // also the chord half-widths hxt[|dz| * 32 + |dy|] = isqrt(r2 - dz^2 - dy^2)
+        // also the chord half-widths hxt[|dz| * kHxStride + |dy|] = isqrt(r2 - dz^2 - dy^2)
         for (int i = tid; i <= rad; i += kFillThreads) hyt[i] = (uint16_t)isqrt24((uint32_t)(R - i * i));
         if (rad <= kHxMax) {
           for (int i = tid; i < (rad + 1) * 32; i += kFillThreads) {
             const int a = i >> 5, c = i & 31;
             const int t = R - a * a - c * c;
-            hxt[i] = t >= 0 ? (uint8_t)isqrt24((uint32_t)t) : (uint8_t)0;
+            hxt[a * kHxStride + c] = t >= 0 ? (uint8_t)isqrt24((uint32_t)t) : (uint8_t)0;
           }
         }
         if (k % kRotEvery == 0 && k > 0) build_rot(usel, rot, warp, lane, kFillWarps);
@@ -402,24 +409,19 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             const int ya = min(pya, 31), yb = max(min(pyb, 31), ya);
             const int lv = 31 - __clz(yb - ya + 1);  // 2^lv <= span
             const uint32_t* tl = rot + (max(lv - 1, 0) * kFillTZ + zc) * kRotStride;
-            const uint32_t orr = lv == 0 ? usel[zc * kFillTY + ya] : (tl[ya] | tl[yb - (1 << lv) + 1]);
+            const uint32_t orr = lv == 0 ? usel[urow(zc, ya)] : (tl[ya] | tl[yb - (1 << lv) + 1]);
             return ok && (orr & range_mask(min(max(xa, 0), 31), max(min(xb, 31), min(max(xa, 0), 31)))) != 0u;
           };
-          // items: (window index, rows ya .. ya + n - 1, plane); planes of at
-          // most 16 rows go to the half-warp list at the top of the array
+          // items: (window index, rows ya .. ya + n, plane)
           auto append = [&](uint32_t bi, bool pass, int pya, int pyb, int zz) {
-            const bool wide = pass && pyb - pya >= 16;
-            const unsigned act_w = __ballot_sync(0xffffffffu, wide);
-            const unsigned act_n = __ballot_sync(0xffffffffu, pass && !wide);
-            if (act_w | act_n) {
+            const unsigned act = __ballot_sync(0xffffffffu, pass);
+            if (act) {
               uint32_t base = 0;
-              if (lane == 0)
-                base = atomicAdd(&s_nitem[parity], (uint32_t)__popc(act_w) | ((uint32_t)__popc(act_n) << 16));
+              if (lane == 0) base = atomicAdd(&s_nitem[parity], (uint32_t)__popc(act));
               base = __shfl_sync(0xffffffffu, base, 0);
-              const uint32_t q =
-                  ((wb + bi) << 14) | ((uint32_t)(pyb - pya) << 9) | ((uint32_t)pya << 4) | (uint32_t)zz;
-              if (wide) item[(base & 0xffffu) + __popc(act_w & lanes_below)] = q;
-              else if (pass) item[kItems - 1 - ((base >> 16) + __popc(act_n & lanes_below))] = q;
+              if (pass)
+                item[base + __popc(act & lanes_below)] =
+                    ((wb + bi) << 14) | ((uint32_t)(pyb - pya) << 9) | ((uint32_t)pya << 4) | (uint32_t)zz;
             }
           };
           for (uint32_t bp = 4 * warp; bp < se - ss; bp += 4 * kFillWarps) {
@@ -431,39 +433,43 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             append(b2, p2, ya2, yb2, z2);
           }
           __syncthreads();
-          // paint: the round's items over all warps, one row per lane (wide
-          // planes) or per half-warp lane (planes of at most 16 rows)
-          const uint32_t packed = s_nitem[parity];
+          // paint: G threads per item (G = 1 .. 8, as many as keep the CTA's
+          // threads busy), each walking every G-th row of the plane's disk
+          // and painting the row's chord of still-unpainted voxels.  Most
+          // items that passed the range-OR test find nothing in any row.
+          const uint32_t nitem = s_nitem[parity];
           if (tid == 0) s_nitem[parity ^ 1u] = 0u;  // the next round's counter (idle since the last barrier)
-          const uint32_t nwide = packed & 0xffffu, nnarrow = packed >> 16;
-          auto paint_row = [&](uint32_t q, int j) {  // row ya + j of item q
-            const int zz = (int)(q & 15u), ya = (int)((q >> 4) & 31u);
-            if (j > (int)((q >> 9) & 31u)) return;
-            const int y = ya + j;
+          const int lg = nitem >= kFillThreads ? 0 : nitem >= kFillThreads / 2 ? 1 : nitem >= kFillThreads / 4 ? 2 : 3;
+          const int G = 1 << lg, sub = tid & (G - 1);
+          for (uint32_t it = (uint32_t)(tid >> lg); it < nitem; it += (uint32_t)(kFillThreads >> lg)) {
+            const uint32_t q = item[it];
+            const int zz = (int)(q & 15u), ya = (int)((q >> 4) & 31u), yb = ya + (int)((q >> 9) & 31u);
             const uint32_t cb = ent[q >> 14];
             const int bx = (int)(cb & 0x3ffu) - 512, by = (int)((cb >> 10) & 0x3ffu) - 512;
-            const int bz = (int)(cb >> 20) - 512;
-            const int dz = zz - bz, dy = y - by;
-            const int t = R - dz * dz - dy * dy;
-            if (t < 0) return;
-            const int row = zz * kFillTY + y;
-            const uint32_t m = usel[row];
-            if (!m) return;
-            const int hx = rad <= kHxMax ? (int)hxt[abs(dz) * 32 + abs(dy)] : (int)isqrt24((uint32_t)t);
-            const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
-            if (xa > xb) return;
-            uint32_t bits = m & range_mask(xa, xb);
-            if (!bits) return;
-            atomicAnd(&usel[row], ~bits);
-            while (bits) {
-              const int xx = __ffs(bits) - 1;
-              val[vidx(row, xx)] = tag;
-              bits &= bits - 1u;
+            const int dz = zz - ((int)(cb >> 20) - 512);
+            const int rz = R - dz * dz;
+            const uint8_t* hxz = hxt + abs(dz) * kHxStride;
+            for (int y = ya + sub; y <= yb; y += G) {
+              const int row = urow(zz, y);
+              const uint32_t m = usel[row];
+              if (!m) continue;
+              const int dy = y - by;
+              const int t = rz - dy * dy;
+              if (t < 0) continue;
+              const int hx = rad <= kHxMax ? (int)hxz[abs(dy)] : (int)isqrt24((uint32_t)t);
+              const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
+              if (xa > xb) continue;
+              uint32_t bits = m & range_mask(xa, xb);
+              if (!bits) continue;
+              atomicAnd(&usel[row], ~bits);
+              const int vrow = zz * kFillTY + y;
+              while (bits) {
+                const int xx = __ffs(bits) - 1;
+                val[vidx(vrow, xx)] = tag;
+                bits &= bits - 1u;
+              }
             }
-          };
-          for (uint32_t it = warp; it < nwide; it += kFillWarps) paint_row(item[it], lane);
-          for (uint32_t it = 2 * warp + half; it < ((nnarrow + 1u) & ~1u); it += 2 * kFillWarps)
-            if (it < nnarrow) paint_row(item[kItems - 1 - it], hl);
+          }
           parity ^= 1u;
           __syncthreads();
           ss = se;
