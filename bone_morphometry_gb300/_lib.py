@@ -14,6 +14,7 @@ import threading
 from . import build as _build
 
 BM_OK = 0
+BM_SITES_AUTO, BM_SITES_SPHERES, BM_SITES_CHAINS = 0, 1, 2
 BM_ERR_ALL_SELECTED = 1
 BM_ERR_DIMS = 2
 BM_ERR_OOM = 3
@@ -131,6 +132,7 @@ SIGNATURES = {
     "bm_server_destroy": (None, [_vp]),
     "bm_footprint_bytes": (ctypes.c_uint64, [_sz, _sz, _sz]),
     "bm_ctx_set_concurrent_phases": (_i, [_vp, _i]),
+    "bm_ctx_set_site_method": (_i, [_vp, _i]),
     "bm_tiff_read": (_i, [ctypes.c_char_p, ctypes.c_uint, _i, _vp, _sz, ctypes.POINTER(_sz), ctypes.POINTER(_sz),
                           ctypes.POINTER(_sz)]),
 }
@@ -213,6 +215,11 @@ class Context:
     def set_concurrent_phases(self, on: bool = True) -> None:
         """Tb.Th and Tb.Sp side by side on two streams (default) or one after the other."""
         self.call("bm_ctx_set_concurrent_phases", 1 if on else 0)
+
+    def set_site_method(self, method: int = 0) -> None:
+        """How the fill finds the non-selected voxels ridge spheres reach:
+        BM_SITES_AUTO (0), BM_SITES_SPHERES (1) or BM_SITES_CHAINS (2)."""
+        self.call("bm_ctx_set_site_method", int(method))
 
     def kernel_times(self) -> dict:
         """{family: (launches, total_ms)} of the kernels timed since profile(True)."""

@@ -173,8 +173,13 @@ void ensure_surf(bm_ctx* ctx, uint32_t rmax);
 
 // Sphere fill of one phase into F (u32 r^2 map): tile-owned fill, or the
 // per-ball atomic scatter when the (ball, tile) entry count would not fit u32.
-void fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsigned long long max_ridges,
-                uint32_t rmax, const uint32_t* occ, const uint32_t* selbits, uint32_t* F, cudaStream_t s) {
+// f, g, m: the x, y and z pass outputs (kept for the chain passes); ridgebits:
+// the ridge bitmask; m is free for reuse once the chain_z pass has read it.
+// Returns the map the fill wrote: F, or m's buffer when F is g's (g is still
+// needed by the chain_y pass that follows the fill).
+uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsigned long long max_ridges,
+                     uint32_t rmax, const uint32_t* occ, const uint32_t* selbits, const uint32_t* f,
+                     const uint32_t* g, uint32_t* m, const uint32_t* ridgebits, uint32_t* F, cudaStream_t s) {
   const size_t rwords = (size_t)rmax + 2;
   uint32_t* rank = static_cast<uint32_t*>(ensure(ctx, ctx->rank, rwords * 4, "r2 ranks"));
   uint32_t* rvals = static_cast<uint32_t*>(ensure(ctx, ctx->rvals, rwords * 4, "r2 values"));
@@ -207,7 +212,7 @@ void fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsign
     check(ctx, cudaMemsetAsync(F, 0, (size_t)dm.n() * 4, s), "memset");
     timed(ctx, KF_FILL, s, "fill kernel",
           [&] { return launch_fill(ridges, ctr, max_ridges, dm, F, s, &ctx->launches); });
-    return;
+    return F;
   }
   uint32_t* entries = static_cast<uint32_t*>(
       ensure(ctx, ctx->binentries, ((size_t)hi.total_entries + 1) * 4, "bin entries"));
@@ -216,14 +221,38 @@ void fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, unsign
       return launch_bin(false, ridges, ctr, max_ridges, rank, info, dm, counts, offsets, entries, s, &ctx->launches);
     });
   }
-  ensure_surf(ctx, rmax);
+  // Sites: lattice points of every ridge sphere (about 2 pi r each, ~2.5 ps a
+  // point), or the two chain passes (~10-16 ps a voxel on 512^3 and 1024^3,
+  // bounded halo): chains once the spheres hold 5 points per voxel
+  const int halo = (int)std::sqrt((double)rmax) + 1;
+  const double sphere_points = 6.283185307179586 * (double)hi.rad_sum;
+  const bool chains_fit = f && g && m && ridgebits && halo <= kChainMaxHalo;
+  const bool chains = chains_fit && (ctx->site_method == BM_SITES_CHAINS ||
+                                     (ctx->site_method == BM_SITES_AUTO && sphere_points > 5.0 * (double)dm.n()));
+  uint32_t* chain = nullptr;
+  if (chains) {
+    const size_t nbytes = (size_t)dm.n() * 4;
+    chain = static_cast<uint32_t*>(ensure(ctx, ctx->chainmap, nbytes, "chain map"));
+    check(ctx, cudaMemsetAsync(chain, 0, nbytes, s), "memset");
+    timed(ctx, KF_FILL_SITES, s, "chain z pass",
+          [&] { return launch_chain_z(g, m, ridgebits, chain, dm, halo, s, &ctx->launches); });
+    if (F == g) F = m;  // the z pass output has been read; g must outlive the fill
+  } else {
+    ensure_surf(ctx, rmax);
+  }
   timed(ctx, KF_FILL, s, "tile fill kernel", [&] {
     return launch_tile_fill(entries, offsets, rvals, rgeo, info, selbits, dm, F, s, &ctx->launches);
   });
-  timed(ctx, KF_FILL_SITES, s, "site kernel", [&] {
-    return launch_sites(ridges, ctr, max_ridges, selbits, static_cast<const uint32_t*>(ctx->surf_off.ptr),
-                        static_cast<const uint32_t*>(ctx->surf_pts.ptr), dm, F, s, &ctx->launches);
-  });
+  if (chains) {
+    timed(ctx, KF_FILL_SITES, s, "chain y pass",
+          [&] { return launch_chain_y(f, g, chain, selbits, F, dm, halo, s, &ctx->launches); });
+  } else {
+    timed(ctx, KF_FILL_SITES, s, "site kernel", [&] {
+      return launch_sites(ridges, ctr, max_ridges, selbits, static_cast<const uint32_t*>(ctx->surf_off.ptr),
+                          static_cast<const uint32_t*>(ctx->surf_pts.ptr), dm, F, s, &ctx->launches);
+    });
+  }
+  return F;
 }
 
 // Lattice points of every sphere |d|^2 = r2 for r2 <= rmax, cached per context.
@@ -286,7 +315,10 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   uint8_t* redo = static_cast<uint8_t*>(ensure(ctx, ctx->redo, redo_bytes, "line flags"));
   timed(ctx, KF_EDT_Y, s, "edt y pass",
         [&] { return launch_edt_window(1, A, B, dm, scratch, redo, ctr, s, &ctx->launches); });
-  uint32_t* E = d_edt ? d_edt : A;
+  // local thickness keeps the x pass output (the chain passes read it): the z
+  // pass then writes its own map
+  uint32_t* E = d_edt ? d_edt
+                      : (edt_only ? A : static_cast<uint32_t*>(ensure(ctx, ctx->edtmap, N * 4, "distance map")));
   timed(ctx, KF_EDT_Z, s, "edt z pass",
         [&] { return launch_edt_window(2, B, E, dm, scratch, redo, ctr, s, &ctx->launches); });
 
@@ -311,10 +343,13 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   const size_t rwords = (size_t)hc.rmax + 2;
   uint32_t* occ = static_cast<uint32_t*>(ensure(ctx, ctx->occ, rwords * 4, "r2 flags"));
   check(ctx, cudaMemsetAsync(occ, 0, rwords * 4, s), "memset");
+  uint32_t* rbits = static_cast<uint32_t*>(ensure(ctx, ctx->ridgebits, bits_bytes, "ridge bits"));
+  check(ctx, cudaMemsetAsync(rbits, 0, bits_bytes, s), "memset");
   timed(ctx, KF_RIDGE, s, "ridge kernel",
-        [&] { return launch_ridges(E, selbits, dm, lut, ridges, ctr, occ, s, &ctx->launches); });
-  uint32_t* F = d_sq ? d_sq : B;
-  fill_phase(ctx, dm, ridges, ctr, res.selected, hc.rmax, occ, selbits, F, s);
+        [&] { return launch_ridges(E, selbits, dm, lut, ridges, ctr, occ, rbits, s, &ctx->launches); });
+  const bool own_e = E != A && E != d_edt;  // E is the context's map: the chain passes may reuse it
+  uint32_t* F = fill_phase(ctx, dm, ridges, ctr, res.selected, hc.rmax, occ, selbits, A, B, own_e ? E : nullptr,
+                           rbits, d_sq ? d_sq : B, s);
   StatsAccum* acc = static_cast<StatsAccum*>(ensure(ctx, ctx->accum, sizeof(StatsAccum), "stats"));
   check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
   FixedPartial* part = static_cast<FixedPartial*>(
@@ -614,6 +649,7 @@ bm_ctx* twin_of(bm_ctx* ctx) {
   const int st = bm_ctx_create(ctx->device, &t);
   if (st != BM_OK) fail(ctx, st, "second stream context creation failed");
   t->profiling = ctx->profiling;
+  t->site_method = ctx->site_method;
   ctx->twin = t;
   return t;
 }
@@ -724,14 +760,19 @@ namespace bm {
 // entry points that take no context).
 void set_thread_error(const char* msg) { g_create_error = msg; }
 
+// The per-call working buffers of a context (released by bm_ctx_trim; the
+// cached tables stay).
+std::vector<Buffer*> work_buffers(bm_ctx* ctx) {
+  return {&ctx->in_a,      &ctx->in_b,       &ctx->dist,        &ctx->dist2,   &ctx->stack,  &ctx->edtmap,
+          &ctx->chainmap,  &ctx->fillmap,    &ctx->selbits,     &ctx->ridgebits, &ctx->ridges, &ctx->accum,
+          &ctx->cpart,     &ctx->outmap,     &ctx->outmap2,     &ctx->occ,     &ctx->rank,   &ctx->rvals,
+          &ctx->bincounts, &ctx->binoffsets, &ctx->binentries,  &ctx->scanscratch, &ctx->redo, &ctx->qhist,
+          &ctx->qtargets,  &ctx->qmap,       &ctx->rgeo};
+}
+
 size_t cached_bytes(const bm_ctx* ctx) {
-  const Buffer* all[] = {&ctx->in_a,     &ctx->in_b,       &ctx->dist,       &ctx->dist2,       &ctx->stack,
-                         &ctx->fillmap,  &ctx->selbits,    &ctx->posbits,    &ctx->ridges,      &ctx->accum,      &ctx->cpart,
-                         &ctx->outmap,   &ctx->outmap2,    &ctx->occ,        &ctx->rank,        &ctx->rvals,
-                         &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
-                         &ctx->qhist,    &ctx->qtargets,   &ctx->qmap,       &ctx->rgeo};
   size_t t = 0;
-  for (const Buffer* b : all) t += b->bytes;
+  for (const Buffer* b : work_buffers(const_cast<bm_ctx*>(ctx))) t += b->bytes;
   if (ctx->twin) t += cached_bytes(ctx->twin);
   return t;
 }
@@ -773,12 +814,7 @@ int bm_ctx_trim(bm_ctx* ctx) {
   return guarded(ctx, [&]() -> int {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->twin) bm_ctx_trim(ctx->twin);
-    Buffer* all[] = {&ctx->in_a,  &ctx->in_b,      &ctx->dist,       &ctx->dist2,      &ctx->stack,
-                     &ctx->fillmap, &ctx->selbits,  &ctx->posbits,   &ctx->ridges,     &ctx->accum,      &ctx->cpart,
-                     &ctx->outmap, &ctx->outmap2,  &ctx->occ,       &ctx->rank,       &ctx->rvals,
-                     &ctx->bincounts, &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
-                     &ctx->qhist, &ctx->qtargets, &ctx->qmap, &ctx->rgeo};
-    for (Buffer* b : all) release(*b);
+    for (Buffer* b : work_buffers(ctx)) release(*b);
     return BM_OK;
   });
 }
@@ -797,13 +833,8 @@ void bm_ctx_destroy(bm_ctx* ctx) {
     if (ctx->twin) bm_ctx_destroy(ctx->twin);
     ctx->twin = nullptr;
     if (ctx->inputs_ready) cudaEventDestroy(ctx->inputs_ready);
-    Buffer* all[] = {&ctx->lut,      &ctx->in_a,      &ctx->in_b,       &ctx->dist,     &ctx->dist2,
-                     &ctx->stack,    &ctx->fillmap,   &ctx->selbits,    &ctx->posbits,  &ctx->ridges,
-                     &ctx->counters, &ctx->accum,     &ctx->cpart,     &ctx->outmap,     &ctx->outmap2,  &ctx->host_pinned,
-                     &ctx->occ,      &ctx->rank,      &ctx->rvals,      &ctx->fillinfo, &ctx->bincounts,
-                     &ctx->binoffsets, &ctx->binentries, &ctx->scanscratch, &ctx->redo,
-                     &ctx->qhist,    &ctx->qtargets,  &ctx->qmap,     &ctx->rgeo};
-    for (Buffer* b : all) release(*b);
+    for (Buffer* b : work_buffers(ctx)) release(*b);
+    for (Buffer* b : {&ctx->lut, &ctx->counters, &ctx->host_pinned, &ctx->fillinfo}) release(*b);
     for (const ProfRec& r : ctx->prof) {
       cudaEventDestroy(r.start);
       cudaEventDestroy(r.stop);
@@ -853,6 +884,16 @@ uint64_t bm_ctx_launch_count(const bm_ctx* ctx) { return ctx ? ctx->launches : 0
 int bm_ctx_set_concurrent_phases(bm_ctx* ctx, int on) {
   return guarded(ctx, [&]() -> int {
     ctx->split_phases = on != 0;
+    return BM_OK;
+  });
+}
+
+int bm_ctx_set_site_method(bm_ctx* ctx, int method) {
+  return guarded(ctx, [&]() -> int {
+    if (method != BM_SITES_AUTO && method != BM_SITES_SPHERES && method != BM_SITES_CHAINS)
+      fail(ctx, BM_ERR_INVALID, "site method must be 0 (auto), 1 (spheres) or 2 (chains); got %d", method);
+    ctx->site_method = method;
+    if (ctx->twin) ctx->twin->site_method = method;
     return BM_OK;
   });
 }

@@ -54,6 +54,20 @@ struct FastDiv {
 #endif
 };
 
+#ifdef __CUDACC__
+// floor(sqrt(v)) for v < 2^30 from the hardware reciprocal square root: the
+// estimate (float)v * rsqrt((float)v) is within 0.01 of sqrt(v) there (the
+// float conversion and the reciprocal root are each within a few ulp), so one
+// integer correction step each way makes the floor exact.
+__device__ __forceinline__ uint32_t isqrt30(uint32_t v) {
+  const float f = (float)v;
+  uint32_t r = (uint32_t)(f * rsqrtf(fmaxf(f, 1.0f)));
+  r -= (r * r > v) ? 1u : 0u;
+  r += ((r + 1) * (r + 1) <= v) ? 1u : 0u;
+  return r;
+}
+#endif
+
 // Linear voxel index -> (x, y, z) without hardware division.
 struct VoxelDecoder {
   FastDiv w, wh;
@@ -119,6 +133,7 @@ struct FillInfo {
   uint32_t nR;                         // distinct ridge r^2 values
   uint32_t pad;
   unsigned long long total_entries;    // (ball, tile) pairs
+  unsigned long long rad_sum;          // sum over ridges of ceil(sqrt(r^2)): about 1/(2 pi) of their sphere points
 };
 
 // Device scratch owned by a context, grown on demand and reused across calls.
@@ -132,7 +147,7 @@ struct Counters {  // device-side counters of one phase
   unsigned long long selected;  // selected voxels
   unsigned long long ridges;
   unsigned int rmax;
-  unsigned int status;  // nonzero: a bounded wait gave up / capacity exceeded
+  unsigned int status;          // nonzero: a bounded wait gave up / capacity exceeded
 };
 
 // Kernel families timed by the context's profiler (bm_profile_*).
@@ -170,6 +185,7 @@ struct bm_ctx {
   bm_ctx* twin = nullptr;
   cudaEvent_t inputs_ready = nullptr;
   bool split_phases = true;  // false: both phases on this context, one after the other
+  int site_method = 0;       // BM_SITES_*
   std::mutex mu;
   std::string last_error;
   unsigned long long launches = 0;
@@ -182,9 +198,10 @@ struct bm_ctx {
 
   bm::Buffer in_a, in_b;       // staged host inputs
   bm::Buffer dist, dist2;      // u32 EDT ping/pong
+  bm::Buffer edtmap, chainmap; // u32 z-pass output kept apart from the x pass's, and the site-chain map
   bm::Buffer stack;            // EDT line scratch
   bm::Buffer fillmap;          // u32 propagated r^2
-  bm::Buffer selbits, posbits; // row-padded bitmasks
+  bm::Buffer selbits, ridgebits; // row-padded bitmasks: selected voxels, ridge voxels
   bm::Buffer ridges;           // ridge records
   bm::Buffer counters;         // bm::Counters
   bm::Buffer accum;            // bm::StatsAccum

@@ -36,17 +36,7 @@ namespace bm {
 
 namespace {
 
-// floor(sqrt(v)) for v < 2^30 from the hardware reciprocal square root: the
-// estimate (float)v * rsqrt((float)v) is within 0.01 of sqrt(v) there (the
-// float conversion and the reciprocal root are each within a few ulp), so one
-// integer correction step each way makes the floor exact.
-__device__ __forceinline__ uint32_t isqrt_u32(uint32_t v) {
-  const float f = (float)v;
-  uint32_t r = (uint32_t)(f * rsqrtf(fmaxf(f, 1.0f)));
-  r -= (r * r > v) ? 1u : 0u;
-  r += ((r + 1) * (r + 1) <= v) ? 1u : 0u;
-  return r;
-}
+__device__ __forceinline__ uint32_t isqrt_u32(uint32_t v) { return isqrt30(v); }  // floor sqrt, v < 2^30
 
 __device__ __forceinline__ uint32_t csqrt_u32(uint32_t v) {
   const uint32_t f = isqrt_u32(v);
@@ -142,7 +132,7 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
            const uint32_t* __restrict__ offsets, uint32_t* __restrict__ entries) {
   const unsigned long long nr = ctr->ridges;
   const uint32_t nR = info->nR;
-  unsigned long long touched = 0;
+  unsigned long long touched = 0, rads = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (long long)nr;
        i += (long long)gridDim.x * blockDim.x) {
     const uint2 rec = ridges[i];
@@ -151,6 +141,7 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
     vd(rec.x, x, y, z);
     const int rad = (int)csqrt_u32(R);
     const uint32_t rank = rank_desc[R];
+    rads += (unsigned)rad;
     const int tx0 = max(x - rad, 0) / kFillTX, tx1 = min(x + rad, dm.w - 1) / kFillTX;
     const int ty0 = max(y - rad, 0) / kFillTY, ty1 = min(y + rad, dm.h - 1) / kFillTY;
     const int tz0 = max(z - rad, 0) / kFillTZ, tz1 = min(z + rad, dm.d - 1) / kFillTZ;
@@ -181,8 +172,12 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
   }
   if (COUNT) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) touched += __shfl_xor_sync(0xffffffffu, touched, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      touched += __shfl_xor_sync(0xffffffffu, touched, o);
+      rads += __shfl_xor_sync(0xffffffffu, rads, o);
+    }
     if ((threadIdx.x & 31) == 0 && touched) atomicAdd(&info->total_entries, touched);
+    if ((threadIdx.x & 31) == 0 && rads) atomicAdd(&info->rad_sum, rads);
   }
 }
 
@@ -258,8 +253,8 @@ constexpr size_t kTileFillSmemWords = (size_t)kRows * 16 + kRows + (kBinChunk + 
 // 1 to 8 threads per item (more when the round has few items) walks the
 // disk's rows and paints each row's chord of unpainted voxels.  Balls of one
 // bin have the same r^2, so the order of their items does not matter (two
-// threads may write the same tag).  Non-selected voxels are left 0
-// here; the site pass adds the ones a sphere reaches.
+// threads may write the same tag).  Non-selected voxels are left 0 here;
+// the site pass or the chain passes add the ones a sphere reaches.
 __global__ void __launch_bounds__(kFillThreads, 4)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
                  const uint32_t* __restrict__ rvals, const uint4* __restrict__ rgeo, const FillInfo* __restrict__ info,
@@ -433,13 +428,13 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             append(b2, p2, ya2, yb2, z2);
           }
           __syncthreads();
-          // paint: G threads per item (G = 1 .. 8, as many as keep the CTA's
-          // threads busy), each walking every G-th row of the plane's disk
+          // paint: G threads per item (G = 1 .. 8, about twice as many as keep
+          // the CTA's threads busy), each walking every G-th row of the plane's disk
           // and painting the row's chord of still-unpainted voxels.  Most
           // items that passed the range-OR test find nothing in any row.
           const uint32_t nitem = s_nitem[parity];
           if (tid == 0) s_nitem[parity ^ 1u] = 0u;  // the next round's counter (idle since the last barrier)
-          const int lg = nitem >= kFillThreads ? 0 : nitem >= kFillThreads / 2 ? 1 : nitem >= kFillThreads / 4 ? 2 : 3;
+          const int lg = nitem >= 2 * kFillThreads ? 0 : nitem >= kFillThreads ? 1 : nitem >= kFillThreads / 2 ? 2 : 3;
           const int G = 1 << lg, sub = tid & (G - 1);
           for (uint32_t it = (uint32_t)(tid >> lg); it < nitem; it += (uint32_t)(kFillThreads >> lg)) {
             const uint32_t q = item[it];

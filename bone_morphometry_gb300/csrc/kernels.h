@@ -43,9 +43,28 @@ cudaError_t launch_edt_window(int axis, const uint32_t* in, uint32_t* out, Dims 
 cudaError_t launch_lut(uint4* lut, uint32_t lo, uint32_t hi, cudaStream_t s, unsigned long long* launches);
 
 // Distance-ridge extraction: appends {linear index, r2} records and, when occ
-// is not null, sets occ[r2] = 1 for every ridge r2.
+// is not null, sets occ[r2] = 1 for every ridge r2.  When ridgebits is not null, writes the ridge bitmask
+// rows (layout of selbits) of every tile with a selected voxel (the caller
+// zeroes it first).
 cudaError_t launch_ridges(const uint32_t* dist, const uint32_t* selbits, Dims dm, const uint4* lut, uint2* ridges,
-                          Counters* ctr, uint32_t* occ, cudaStream_t s, unsigned long long* launches);
+                          Counters* ctr, uint32_t* occ, uint32_t* ridgebits, cudaStream_t s,
+                          unsigned long long* launches);
+
+// Site values by reverse chain passes: the non-selected voxels a ridge sphere
+// reaches are exactly the nearest sites of the ridge voxel, reached through
+// the argmins of the z, y and x passes.  launch_chain_z: for every ridge
+// voxel c (ridgebits) and every z' with g(x, y, z') + (z - z')^2 = m(c),
+// chain(x, y, z') = max(., m(c)) (chain zeroed by the caller).
+// launch_chain_y: for every (x, y, z') with chain > 0 and every y' with
+// f(x, y', z') + (y - y')^2 = g(x, y, z'), the x pass's nearest sites x' of
+// (x, y', z') get sites(x', y', z') = max(., chain): run on the tile fill's
+// map, whose non-selected voxels are 0, it adds what launch_sites would.  f, g, m: the x, y and z pass outputs.  halo: rows staged on each
+// side, at least isqrt(largest ridge r2) + 1 and at most 64.
+constexpr int kChainMaxHalo = 64;
+cudaError_t launch_chain_z(const uint32_t* g, const uint32_t* m, const uint32_t* ridgebits, uint32_t* chain, Dims dm,
+                           int halo, cudaStream_t s, unsigned long long* launches);
+cudaError_t launch_chain_y(const uint32_t* f, const uint32_t* g, const uint32_t* chain, const uint32_t* selbits,
+                           uint32_t* sites, Dims dm, int halo, cudaStream_t s, unsigned long long* launches);
 
 // Sphere fill: atomic max of r2 over every voxel of each ridge ball (any phase).
 cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long long max_ridges, Dims dm,

@@ -377,7 +377,7 @@ constexpr int kRSX = kRTX + 2, kRSY = kRTY + 2, kRSZ = kRTZ + 2;
 __global__ void __launch_bounds__(256)
 ridge_tile_kernel(const uint32_t* __restrict__ dist, const uint32_t* __restrict__ selbits, Dims dm,
                   const uint4* __restrict__ lut, uint2* __restrict__ ridges, Counters* __restrict__ ctr,
-                  uint32_t* __restrict__ occ, int ntx, int nty, int ntz) {
+                  uint32_t* __restrict__ occ, uint32_t* __restrict__ ridgebits, int ntx, int nty, int ntz) {
   __shared__ uint32_t D[kRSZ * kRSY * kRSX];
   __shared__ uint32_t s_wcnt[8];
   __shared__ unsigned long long s_base;
@@ -453,6 +453,7 @@ ridge_tile_kernel(const uint32_t* __restrict__ dist, const uint32_t* __restrict_
       }
       mk[k] = __ballot_sync(0xffffffffu, ridge);
       wcount += __popc(mk[k]);
+      if (ridgebits && lane == 0 && z < dm.d && y < dm.h) ridgebits[((long long)z * dm.h + y) * nw + tx] = mk[k];
     }
     if (lane == 0) s_wcnt[warp] = (uint32_t)wcount;
     __syncthreads();
@@ -512,11 +513,12 @@ cudaError_t launch_dia_table(const uint4* lut, uint32_t n, float* dia, cudaStrea
 }
 
 cudaError_t launch_ridges(const uint32_t* dist, const uint32_t* selbits, Dims dm, const uint4* lut, uint2* ridges,
-                          Counters* ctr, uint32_t* occ, cudaStream_t s, unsigned long long* launches) {
+                          Counters* ctr, uint32_t* occ, uint32_t* ridgebits, cudaStream_t s,
+                          unsigned long long* launches) {
   const int ntx = (dm.w + kRTX - 1) / kRTX, nty = (dm.h + kRTY - 1) / kRTY, ntz = (dm.d + kRTZ - 1) / kRTZ;
   const long long tiles = (long long)ntx * nty * ntz;
   ridge_tile_kernel<<<resident_grid(ridge_tile_kernel, 256, 0, tiles), 256, 0, s>>>(dist, selbits, dm, lut, ridges,
-                                                                                    ctr, occ, ntx, nty, ntz);
+                                                                                    ctr, occ, ridgebits, ntx, nty, ntz);
   ++*launches;
   return cudaGetLastError();
 }

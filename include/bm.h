@@ -272,6 +272,16 @@ int bm_tiff_read(const char* path, unsigned threshold, int accepted, uint8_t* ou
  * alone).  Results are identical either way. */
 int bm_ctx_set_concurrent_phases(bm_ctx* ctx, int on);
 
+/* How the sphere fill finds the non-selected voxels a ridge ball reaches
+ * (local_thickness.rs:169-202 paints them too): BM_SITES_SPHERES tests every
+ * lattice point of every ridge sphere; BM_SITES_CHAINS pushes the ridge r^2
+ * backwards along the distance transform's tied argmins (two window passes
+ * over the volume, two more u32 maps of device memory); BM_SITES_AUTO (the
+ * default) picks chains when the spheres would hold more than five lattice
+ * points per voxel of the volume.  Results are identical either way. */
+enum { BM_SITES_AUTO = 0, BM_SITES_SPHERES = 1, BM_SITES_CHAINS = 2 };
+int bm_ctx_set_site_method(bm_ctx* ctx, int method);
+
 /* Kernel launches issued by this context since creation (library kernels only). */
 uint64_t bm_ctx_launch_count(const bm_ctx* ctx);
 

@@ -106,9 +106,17 @@ LT_CASES = [
 ]
 
 
+@pytest.fixture(params=[_lib.BM_SITES_SPHERES, _lib.BM_SITES_CHAINS], ids=["spheres", "chains"])
+def site_method(request, gpu_ctx):
+    """Both ways of finding the non-selected voxels a ridge sphere reaches."""
+    gpu_ctx.set_site_method(request.param)
+    yield request.param
+    gpu_ctx.set_site_method(_lib.BM_SITES_AUTO)
+
+
 @pytest.mark.parametrize("kind,args", LT_CASES)
 @pytest.mark.parametrize("phase", [Phase.FOREGROUND, Phase.BACKGROUND])
-def test_local_thickness_bitwise(gpu_ctx, kind, args, phase):
+def test_local_thickness_bitwise(gpu_ctx, site_method, kind, args, phase):
     if kind == "kat":
         vol = np.zeros((3, 3, 3), np.uint8)
         vol[1, 1, 1] = 1
@@ -124,7 +132,7 @@ def test_local_thickness_bitwise(gpu_ctx, kind, args, phase):
     assert np.array_equal(got.view(np.uint32), ref.thickness.view(np.uint32))
 
 
-def test_local_thickness_huge_balls(gpu_ctx):
+def test_local_thickness_huge_balls(gpu_ctx, site_method):
     # one site in a corner: r^2 up to ~3000, balls spanning many fill tiles
     vol = np.ones((24, 30, 36), np.uint8)
     vol[0, 0, 0] = 0
@@ -165,7 +173,7 @@ def check_stats(got, ref_map, scale):
     assert abs(got.standard_deviation - seq.sd) <= seq_tol(n, amp) * abs(seq.sd) + 1e-300
 
 
-def test_tbth_tbsp_plain_128(gpu_ctx):
+def test_tbth_tbsp_plain_128(gpu_ctx, site_method):
     sp = S.config_plain_128()
     res = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx, return_maps=True)
     for sel, got, gmap in ((True, res.thickness, res.thickness_map), (False, res.spacing, res.spacing_map)):
@@ -176,7 +184,7 @@ def test_tbth_tbsp_plain_128(gpu_ctx):
 
 
 @pytest.mark.parametrize("seed", [21, 22])
-def test_tbth_tbsp_small_random_specimens(gpu_ctx, seed):
+def test_tbth_tbsp_small_random_specimens(gpu_ctx, site_method, seed):
     rng = np.random.default_rng(seed)
     shape = tuple(int(v) for v in rng.integers(20, 70, size=3))
     sp = S.make_specimen(shape, float(rng.uniform(1.5, 3)), float(rng.uniform(0.1, 0.4)), "cylinder",
