@@ -351,8 +351,16 @@ def bench_serving(n_requests=64, rate=200.0, budget=120e9, workers=(2, 4)):
         lat_serial.append(end - t_arr[i])
     span_serial = end - t_arr[0]
     # served
+    by_size = sorted(range(len(pool)), key=lambda k: -pool[k].bone.size)
+
     def serve(nworkers):
         with Server(workers=nworkers, hbm_budget_bytes=budget) as srv:
+            # warm the workers (device buffers grown to the largest specimen,
+            # tables built): every specimen once, the largest once per worker
+            warm = [srv.submit(pool[k].bone, pool[k].roi, pool[k].spacing_um)
+                    for k in [by_size[0]] * nworkers + by_size]
+            for t in warm:
+                srv.result(t)
             tickets = []
             t_start = time.perf_counter()
             for i, k in enumerate(order):

@@ -282,10 +282,11 @@ extern "C" {
 
 uint64_t bm_footprint_bytes(size_t width, size_t height, size_t depth) {
   // per voxel: inputs 2; per phase (the two phases run side by side, each on
-  // its own buffers): two u32 maps 8, envelope scratch 8, ridge records <= 8,
-  // bin entries ~5, quantile map 4, bitmasks ~1; tables 2 x 64 MiB
+  // its own buffers): four u32 maps 16 (x/y pass, z pass, chain map), envelope
+  // scratch 8, ridge records <= 8, bin entries ~5, quantile map 4, bitmasks ~1;
+  // tables 2 x 64 MiB
   const uint64_t n = (uint64_t)width * height * depth;
-  return n * 70u + (128ull << 20);
+  return n * 86u + (128ull << 20);
 }
 
 int bm_ctx_set_workers(bm_ctx* ctx, int workers) {
