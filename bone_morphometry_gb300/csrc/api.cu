@@ -221,14 +221,16 @@ uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, u
       return launch_bin(false, ridges, ctr, max_ridges, rank, info, dm, counts, offsets, entries, s, &ctx->launches);
     });
   }
-  // Sites: lattice points of every ridge sphere (about 2 pi r each, ~2.5 ps a
-  // point), or the two chain passes (~10-16 ps a voxel on 512^3 and 1024^3,
-  // bounded halo): chains once the spheres hold 5 points per voxel
+  // Sites: the site kernel's half-warp steps over the ridge spheres' lattice
+  // points (35-55 ps each, measured), or the two chain passes (9-17 ps a
+  // voxel, bounded halo): chains above 0.2 steps per voxel.  The 512^3
+  // workload's phases sit at 0.07 (bone) and 0.62 (marrow), the 1024^3
+  // plate generator's at 0.10 and 0.28.
   const int halo = (int)std::sqrt((double)rmax) + 1;
-  const double sphere_points = 6.283185307179586 * (double)hi.rad_sum;
   const bool chains_fit = f && g && m && ridgebits && halo <= kChainMaxHalo;
+  const bool auto_chains = (double)hi.site_steps > 0.2 * (double)dm.n();
   const bool chains = chains_fit && (ctx->site_method == BM_SITES_CHAINS ||
-                                     (ctx->site_method == BM_SITES_AUTO && sphere_points > 5.0 * (double)dm.n()));
+                                     (ctx->site_method == BM_SITES_AUTO && auto_chains));
   uint32_t* chain = nullptr;
   if (chains) {
     const size_t nbytes = (size_t)dm.n() * 4;

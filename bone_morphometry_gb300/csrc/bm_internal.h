@@ -133,7 +133,8 @@ struct FillInfo {
   uint32_t nR;                         // distinct ridge r^2 values
   uint32_t pad;
   unsigned long long total_entries;    // (ball, tile) pairs
-  unsigned long long rad_sum;          // sum over ridges of ceil(sqrt(r^2)): about 1/(2 pi) of their sphere points
+  unsigned long long site_steps;       // sum over ridges of ceil(2 pi ceil(sqrt(r^2)) / 16): half-warp steps of
+                                       // the site kernel over the spheres' lattice points (about 2 pi r each)
 };
 
 // Device scratch owned by a context, grown on demand and reused across calls.

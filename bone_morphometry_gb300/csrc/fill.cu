@@ -132,7 +132,7 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
            const uint32_t* __restrict__ offsets, uint32_t* __restrict__ entries) {
   const unsigned long long nr = ctr->ridges;
   const uint32_t nR = info->nR;
-  unsigned long long touched = 0, rads = 0;
+  unsigned long long touched = 0, steps = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (long long)nr;
        i += (long long)gridDim.x * blockDim.x) {
     const uint2 rec = ridges[i];
@@ -141,7 +141,7 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
     vd(rec.x, x, y, z);
     const int rad = (int)csqrt_u32(R);
     const uint32_t rank = rank_desc[R];
-    rads += (unsigned)rad;
+    steps += ((unsigned)rad * 402u + 1023u) >> 10;  // ceil(2 pi rad / 16): 2 pi / 16 ~ 402 / 1024
     const int tx0 = max(x - rad, 0) / kFillTX, tx1 = min(x + rad, dm.w - 1) / kFillTX;
     const int ty0 = max(y - rad, 0) / kFillTY, ty1 = min(y + rad, dm.h - 1) / kFillTY;
     const int tz0 = max(z - rad, 0) / kFillTZ, tz1 = min(z + rad, dm.d - 1) / kFillTZ;
@@ -174,10 +174,10 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       touched += __shfl_xor_sync(0xffffffffu, touched, o);
-      rads += __shfl_xor_sync(0xffffffffu, rads, o);
+      steps += __shfl_xor_sync(0xffffffffu, steps, o);
     }
     if ((threadIdx.x & 31) == 0 && touched) atomicAdd(&info->total_entries, touched);
-    if ((threadIdx.x & 31) == 0 && rads) atomicAdd(&info->rad_sum, rads);
+    if ((threadIdx.x & 31) == 0 && steps) atomicAdd(&info->site_steps, steps);
   }
 }
 
@@ -201,7 +201,7 @@ constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the rang
 constexpr int kRotStride = 33;    // words per range-OR row: lanes testing different planes hit different banks
 constexpr int kItems = 1024;      // (ball, plane) paint items per round
 constexpr int kHxMax = 31;        // balls up to this radius read their chord half-widths from a table
-constexpr int kHxStride = 36;     // bytes per |dz| row of that table (9 words: rows of consecutive planes in different banks)
+constexpr int kHxStride = 36;     // bytes per |dz| row of that table (9 words: consecutive planes, other banks)
 constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
 
 // rot[lv - 1][z][y] (rows of kRotStride words) = OR of the unpainted-voxel

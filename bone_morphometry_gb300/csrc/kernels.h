@@ -58,8 +58,9 @@ cudaError_t launch_ridges(const uint32_t* dist, const uint32_t* selbits, Dims dm
 // launch_chain_y: for every (x, y, z') with chain > 0 and every y' with
 // f(x, y', z') + (y - y')^2 = g(x, y, z'), the x pass's nearest sites x' of
 // (x, y', z') get sites(x', y', z') = max(., chain): run on the tile fill's
-// map, whose non-selected voxels are 0, it adds what launch_sites would.  f, g, m: the x, y and z pass outputs.  halo: rows staged on each
-// side, at least isqrt(largest ridge r2) + 1 and at most 64.
+// map, whose non-selected voxels are 0, it adds what launch_sites would.
+// f, g, m: the x, y and z pass outputs.  halo: rows staged on each side, at
+// least isqrt(largest ridge r2) + 1 and at most 64.
 constexpr int kChainMaxHalo = 64;
 cudaError_t launch_chain_z(const uint32_t* g, const uint32_t* m, const uint32_t* ridgebits, uint32_t* chain, Dims dm,
                            int halo, cudaStream_t s, unsigned long long* launches);

@@ -277,8 +277,9 @@ int bm_ctx_set_concurrent_phases(bm_ctx* ctx, int on);
  * lattice point of every ridge sphere; BM_SITES_CHAINS pushes the ridge r^2
  * backwards along the distance transform's tied argmins (two window passes
  * over the volume, two more u32 maps of device memory); BM_SITES_AUTO (the
- * default) picks chains when the spheres would hold more than five lattice
- * points per voxel of the volume.  Results are identical either way. */
+ * default) picks chains when the spheres' lattice points would take the site
+ * test more than 0.2 half-warp steps per voxel of the volume.  Results are
+ * identical either way. */
 enum { BM_SITES_AUTO = 0, BM_SITES_SPHERES = 1, BM_SITES_CHAINS = 2 };
 int bm_ctx_set_site_method(bm_ctx* ctx, int method);
 
