@@ -227,7 +227,7 @@ uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, u
   // workload's phases sit at 0.07 (bone) and 0.62 (marrow), the 1024^3
   // plate generator's at 0.10 and 0.28.
   const int halo = (int)std::sqrt((double)rmax) + 1;
-  const bool chains_fit = f && g && m && ridgebits && halo <= kChainMaxHalo;
+  const bool chains_fit = f && g && m && ridgebits && rmax < (uint32_t)kChainMaxR2;
   const bool auto_chains = (double)hi.site_steps > 0.2 * (double)dm.n();
   const bool chains = chains_fit && (ctx->site_method == BM_SITES_CHAINS ||
                                      (ctx->site_method == BM_SITES_AUTO && auto_chains));

@@ -19,8 +19,9 @@
 // Geometry (both passes): a CTA owns 32 consecutive x of one line-row and
 // kChainTL consecutive outputs along the axis, stages the pass input with a
 // halo of H rows on each side (H > isqrt of every minimum pushed, so every
-// argmin lies in the staged rows), accumulates the pushed maxima per staged
-// cell in shared memory and flushes the non-zero cells with global atomics.
+// argmin lies in the staged rows; every pushed minimum and value is below
+// 2^11), accumulates the pushed maxima per staged cell in shared memory and
+// flushes the non-zero cells with global atomics.
 #include "kernels.h"
 
 namespace bm {
@@ -31,6 +32,7 @@ constexpr int kChainTL = 128;
 constexpr int kChainThreads = 256;
 constexpr int kChainWarps = kChainThreads / 32;
 constexpr int kChainPer = kChainTL / kChainWarps;  // outputs per thread (rows warp + 8 j)
+constexpr int kChainRowsPerList = 4;                // rows of a warp compacted into one push list
 
 // AXIS 2 (chain_z): lines along z at y = orow; in = g, outv = m, the pushed
 // value is m at ridge voxels (bits = ridge bitmask); flush into dst = chain.
@@ -47,7 +49,9 @@ chain_kernel(const uint32_t* __restrict__ in, const uint32_t* __restrict__ outv,
   const int rows = kChainTL + 2 * H;
   uint32_t* sin = sm;              // rows x 32: staged input (kInfSq outside the line)
   uint32_t* acc = sm + rows * 32;  // rows x 32: largest value pushed to the cell
-  uint32_t* sel5 = acc + rows * 32;  // AXIS 1: rows x 5 selection words, x words xt-2 .. xt+2 (the x step's sites)
+  uint32_t* lst = acc + rows * 32;  // per warp: the push list (kChainRowsPerList * 32 entries)
+  uint32_t* sel5 = lst + kChainWarps * kChainRowsPerList * 32;  // AXIS 1: rows x 5 selection words, x words
+                                                                 // xt-2 .. xt+2 (the x step's sites)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long bid = blockIdx.x;
   const int xt = (int)(bid % nxt);
@@ -64,10 +68,11 @@ chain_kernel(const uint32_t* __restrict__ in, const uint32_t* __restrict__ outv,
   for (int j = 0; j < kChainPer; ++j) {
     const int q = q0 + warp + kChainWarps * j;
     const bool qin = xin && q < n;
-    if (AXIS == 2) {
+    if (AXIS == 2) {  // only ridge voxels push: the others' minima are not read
       const uint32_t rb = q < n ? bits[((long long)q * dm.h + orow) * nw + xt] : 0u;  // one word per warp
-      o[j] = qin ? outv[base + (long long)q * stride] : 0u;
-      v[j] = (qin && ((rb >> lane) & 1u)) ? o[j] : 0u;
+      const bool ridge = qin && ((rb >> lane) & 1u);
+      o[j] = ridge ? outv[base + (long long)q * stride] : 0u;
+      v[j] = o[j];
     } else {
       v[j] = qin ? val[base + (long long)q * stride] : 0u;
       o[j] = qin ? outv[base + (long long)q * stride] : 0u;
@@ -107,20 +112,41 @@ chain_kernel(const uint32_t* __restrict__ in, const uint32_t* __restrict__ outv,
   }
   __syncthreads();
   // push: every p with in(p) + (q - p)^2 = outv(q) is an argmin of output q;
-  // |q - p| <= isqrt(outv(q)) < H keeps p inside the staged rows
+  // |q - p| <= isqrt(outv(q)) < H keeps p inside the staged rows.  The warp's
+  // outputs that push are compacted (four rows at a time, 128 candidates) so
+  // that every lane scans one whatever the ridge density; an entry packs row
+  // j, column, minimum and value (both below 2^11: the caller's bound)
+  uint32_t* wl = lst + warp * (kChainRowsPerList * 32);
+  const unsigned lanes_below = (1u << lane) - 1u;
 #pragma unroll
-  for (int j = 0; j < kChainPer; ++j) {
-    const uint32_t vq = v[j], oq = o[j];
-    if (vq == 0u || oq >= kInfSq) continue;
-    const int i = H + warp + kChainWarps * j;
-    const uint32_t* col = sin + i * 32 + lane;
-    uint32_t* ac = acc + i * 32 + lane;
-    if (col[0] == oq) atomicMax(ac, vq);
-    for (int dp = 1; (uint32_t)(dp * dp) <= oq && dp < H; ++dp) {
-      const uint32_t need = oq - (uint32_t)(dp * dp);
-      if (col[-dp * 32] == need) atomicMax(ac - dp * 32, vq);
-      if (col[dp * 32] == need) atomicMax(ac + dp * 32, vq);
+  for (int j0 = 0; j0 < kChainPer; j0 += kChainRowsPerList) {
+    int cnt = 0;
+#pragma unroll
+    for (int jj = 0; jj < kChainRowsPerList; ++jj) {
+      const int j = j0 + jj;
+      const bool has = v[j] != 0u && o[j] < kInfSq;
+      const unsigned m = __ballot_sync(0xffffffffu, has);
+      if (has)
+        wl[cnt + __popc(m & lanes_below)] =
+            ((uint32_t)j << 27) | ((uint32_t)lane << 22) | (o[j] << 11) | v[j];
+      cnt += __popc(m);
     }
+    __syncwarp();
+    for (int k = lane; k < cnt; k += 32) {
+      const uint32_t e = wl[k];
+      const int j = (int)(e >> 27), c = (int)((e >> 22) & 31u);
+      const uint32_t oq = (e >> 11) & 2047u, vq = e & 2047u;
+      const int i = H + warp + kChainWarps * j;
+      const uint32_t* col = sin + i * 32 + c;
+      uint32_t* ac = acc + i * 32 + c;
+      if (col[0] == oq) atomicMax(ac, vq);
+      for (int dp = 1; (uint32_t)(dp * dp) <= oq && dp < H; ++dp) {
+        const uint32_t need = oq - (uint32_t)(dp * dp);
+        if (col[-dp * 32] == need) atomicMax(ac - dp * 32, vq);
+        if (col[dp * 32] == need) atomicMax(ac + dp * 32, vq);
+      }
+    }
+    __syncwarp();
   }
   __syncthreads();
   // flush the cells that received a value (the halo cells belong to the
@@ -164,7 +190,8 @@ cudaError_t launch_chain(const uint32_t* in, const uint32_t* outv, const uint32_
   const int nxt = (dm.w + 31) / 32;
   const int nchunk = (n + kChainTL - 1) / kChainTL;
   const long long blocks = (long long)nxt * nchunk * orows;
-  const size_t smem = (size_t)(2 * 32 + (AXIS == 1 ? 5 : 0)) * (kChainTL + 2 * halo) * sizeof(uint32_t);
+  const size_t smem = ((size_t)(2 * 32 + (AXIS == 1 ? 5 : 0)) * (kChainTL + 2 * halo) +
+                       (size_t)kChainWarps * kChainRowsPerList * 32) * sizeof(uint32_t);
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(chain_kernel<AXIS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

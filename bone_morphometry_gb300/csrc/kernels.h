@@ -60,8 +60,10 @@ cudaError_t launch_ridges(const uint32_t* dist, const uint32_t* selbits, Dims dm
 // (x, y', z') get sites(x', y', z') = max(., chain): run on the tile fill's
 // map, whose non-selected voxels are 0, it adds what launch_sites would.
 // f, g, m: the x, y and z pass outputs.  halo: rows staged on each side, at
-// least isqrt(largest ridge r2) + 1 and at most 64.
-constexpr int kChainMaxHalo = 64;
+// least isqrt(largest ridge r2) + 1; the largest ridge r2 must be below
+// kChainMaxR2.
+constexpr int kChainMaxR2 = 2048;
+constexpr int kChainMaxHalo = 46;  // isqrt(kChainMaxR2 - 1) + 1
 cudaError_t launch_chain_z(const uint32_t* g, const uint32_t* m, const uint32_t* ridgebits, uint32_t* chain, Dims dm,
                            int halo, cudaStream_t s, unsigned long long* launches);
 cudaError_t launch_chain_y(const uint32_t* f, const uint32_t* g, const uint32_t* chain, const uint32_t* selbits,

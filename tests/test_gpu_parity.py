@@ -94,6 +94,8 @@ def test_errors(gpu_ctx):
         analyze_thickness(bone, roi, 1.0, ctx=gpu_ctx)
     with pytest.raises(BoneMorphometryError, match="finite and positive"):
         analyze_thickness(bone, roi, float("nan"), ctx=gpu_ctx)
+    with pytest.raises(BoneMorphometryError, match="site method must be"):
+        gpu_ctx.set_site_method(3)
     # the context stays usable after errors
     vol = rand_volume((9, 9, 9), 0.5, 0)
     assert np.array_equal(euclidean_distance_transform_squared(vol, ctx=gpu_ctx), O.edt_sq(vol))
