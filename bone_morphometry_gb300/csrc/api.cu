@@ -130,7 +130,8 @@ Dims check_dims(bm_ctx* ctx, size_t w, size_t h, size_t d) {
   if (n >= 0xFFFFFFFFull)
     fail(ctx, BM_ERR_DIMS, "volume of %llu voxels exceeds the 2^32-1 voxel limit", n);
   const unsigned long long r2 =
-      (unsigned long long)(w - 1) * (w - 1) + (unsigned long long)(h - 1) * (h - 1) + (unsigned long long)(d - 1) * (d - 1);
+      (unsigned long long)(w - 1) * (w - 1) + (unsigned long long)(h - 1) * (h - 1) +
+      (unsigned long long)(d - 1) * (d - 1);
   if (r2 >= (1ull << 30)) fail(ctx, BM_ERR_DIMS, "largest squared distance %llu exceeds 2^30", r2);
   return Dims{(int)w, (int)h, (int)d};
 }

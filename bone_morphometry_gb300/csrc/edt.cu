@@ -619,7 +619,8 @@ cudaError_t launch_edt_x_mode(const uint8_t* a, const uint8_t* b, Dims dm, uint3
                    (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
   if (vec) {
     if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(edt_x_vec_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaError_t e =
+          cudaFuncSetAttribute(edt_x_vec_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
     edt_x_vec_kernel<MODE><<<blocks, kXWarps * 32, smem, s>>>(a, b, dm, out, selbits, ctr);

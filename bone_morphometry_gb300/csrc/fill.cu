@@ -52,7 +52,8 @@ constexpr long long kScanTile = kScanThreads * kScanItems;
 
 // Exclusive scan of one 4096-element tile; writes the tile total to sums.
 __global__ void __launch_bounds__(kScanThreads)
-scan_tile_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, long long n, uint32_t* __restrict__ sums) {
+scan_tile_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, long long n,
+                 uint32_t* __restrict__ sums) {
   __shared__ uint32_t wsum[32];
   const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
   uint32_t v[kScanItems];

@@ -476,7 +476,8 @@ ridge_tile_kernel(const uint32_t* __restrict__ dist, const uint32_t* __restrict_
         const int oz = r / kRTY, oy = r % kRTY;
         const int z = z0 + oz, y = y0 + oy, x = x0 + lane;
         const uint32_t R = D[((oz + 1) * kRSY + oy + 1) * kRSX + lane + 1];
-        ridges[slot + __popc(m & ((1u << lane) - 1u))] = make_uint2((uint32_t)(((long long)z * dm.h + y) * dm.w + x), R);
+        ridges[slot + __popc(m & ((1u << lane) - 1u))] =
+            make_uint2((uint32_t)(((long long)z * dm.h + y) * dm.w + x), R);
         if (occ && occ[R] == 0u) occ[R] = 1u;
       }
       slot += __popc(m);

@@ -116,7 +116,8 @@ cudaError_t launch_moments(const float* map, long long n, float scale, StatsAccu
   return cudaGetLastError();
 }
 
-cudaError_t launch_hist_hi(const float* map, long long n, uint32_t* hist, cudaStream_t s, unsigned long long* launches) {
+cudaError_t launch_hist_hi(const float* map, long long n, uint32_t* hist, cudaStream_t s,
+                           unsigned long long* launches) {
   long long blocks = (n + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (blocks < 1) blocks = 1;
