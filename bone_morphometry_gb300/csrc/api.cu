@@ -250,9 +250,13 @@ uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, u
     timed(ctx, KF_FILL_SITES, s, "chain y pass",
           [&] { return launch_chain_y(f, g, chain, selbits, F, dm, halo, s, &ctx->launches); });
   } else {
+    // 8 lanes per ridge when the spheres average at most 2.5 half-warp steps
+    // (about 40 lattice points): half-warps would idle on their last step
+    const bool small_spheres = 2 * hi.site_steps <= 5 * hi.ridges;
     timed(ctx, KF_FILL_SITES, s, "site kernel", [&] {
       return launch_sites(ridges, ctr, max_ridges, selbits, static_cast<const uint32_t*>(ctx->surf_off.ptr),
-                          static_cast<const uint32_t*>(ctx->surf_pts.ptr), dm, F, s, &ctx->launches);
+                          static_cast<const uint32_t*>(ctx->surf_pts.ptr), small_spheres, dm, F, s,
+                          &ctx->launches);
     });
   }
   return F;

@@ -135,6 +135,7 @@ struct FillInfo {
   unsigned long long total_entries;    // (ball, tile) pairs
   unsigned long long site_steps;       // sum over ridges of ceil(2 pi ceil(sqrt(r^2)) / 16): half-warp steps of
                                        // the site kernel over the spheres' lattice points (about 2 pi r each)
+  unsigned long long ridges;           // ridge count
 };
 
 // Device scratch owned by a context, grown on demand and reused across calls.

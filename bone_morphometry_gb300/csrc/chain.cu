@@ -73,9 +73,9 @@ chain_kernel(const uint32_t* __restrict__ in, const uint32_t* __restrict__ outv,
       const bool ridge = qin && ((rb >> lane) & 1u);
       o[j] = ridge ? outv[base + (long long)q * stride] : 0u;
       v[j] = o[j];
-    } else {
+    } else {  // only cells with a chain value push
       v[j] = qin ? val[base + (long long)q * stride] : 0u;
-      o[j] = qin ? outv[base + (long long)q * stride] : 0u;
+      o[j] = v[j] ? outv[base + (long long)q * stride] : 0u;
     }
   }
   // a block with nothing to push has nothing to flush either

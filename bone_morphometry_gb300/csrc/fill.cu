@@ -179,6 +179,7 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
     }
     if ((threadIdx.x & 31) == 0 && touched) atomicAdd(&info->total_entries, touched);
     if ((threadIdx.x & 31) == 0 && steps) atomicAdd(&info->site_steps, steps);
+    if (blockIdx.x == 0 && threadIdx.x == 0) info->ridges = nr;
   }
 }
 
@@ -488,25 +489,28 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
 // The non-selected voxels a ridge ball reaches.  A ball centred on p has r^2 =
 // d^2(p), the squared distance from p to its nearest non-selected voxel, so the
 // non-selected voxels inside it are exactly the non-selected lattice points of
-// its sphere |v - p|^2 = r^2.  Half a warp per ridge, lanes over the sphere's
-// points; the map keeps the max over balls.  Runs after the tile fill, which
-// leaves every non-selected voxel at 0.
+// its sphere |v - p|^2 = r^2.  G lanes per ridge (16, or 8 when the spheres
+// are small), lanes over the sphere's points; the map keeps the max over
+// balls.  Runs after the tile fill, which leaves every non-selected voxel at 0.
+template <int G>
 __global__ void __launch_bounds__(256)
 site_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, const uint32_t* __restrict__ selbits,
             const uint32_t* __restrict__ surf_off, const uint32_t* __restrict__ surf_pts, Dims dm, VoxelDecoder vd,
             uint32_t* __restrict__ fillmap) {
+  constexpr int kLog = G == 16 ? 4 : 3;
+  static_assert(G == (1 << kLog), "8 or 16 lanes per ridge");
   const unsigned long long nr = ctr->ridges;
-  const int hl = threadIdx.x & 15;
+  const int hl = threadIdx.x & (G - 1);
   const int nw = dm.nw();
-  const long long hw0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 4;
-  const long long nhw = ((long long)gridDim.x * blockDim.x) >> 4;
+  const long long hw0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> kLog;
+  const long long nhw = ((long long)gridDim.x * blockDim.x) >> kLog;
   for (long long i = hw0; i < (long long)nr; i += nhw) {
     const uint2 rec = ridges[i];
     const uint32_t R = rec.y;
     int x, y, z;
     vd(rec.x, x, y, z);
     const uint32_t p1 = surf_off[R + 1];
-    for (uint32_t p = surf_off[R] + hl; p < p1; p += 16) {
+    for (uint32_t p = surf_off[R] + hl; p < p1; p += G) {
       const uint32_t pk = surf_pts[p];
       const int sx = x + ((int)(pk << 22) >> 22);
       const int sy = y + ((int)(pk << 12) >> 22);
@@ -671,10 +675,13 @@ cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, c
 }
 
 cudaError_t launch_sites(const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
-                         const uint32_t* selbits, const uint32_t* surf_off, const uint32_t* surf_pts, Dims dm,
-                         uint32_t* fillmap, cudaStream_t s, unsigned long long* launches) {
-  const unsigned blocks = blocks_for((long long)max_ridges, 16, 152 * 16);
-  site_kernel<<<blocks, 256, 0, s>>>(ridges, ctr, selbits, surf_off, surf_pts, dm, VoxelDecoder::of(dm), fillmap);
+                         const uint32_t* selbits, const uint32_t* surf_off, const uint32_t* surf_pts, bool small,
+                         Dims dm, uint32_t* fillmap, cudaStream_t s, unsigned long long* launches) {
+  const unsigned blocks = blocks_for((long long)max_ridges, small ? 32 : 16, 152 * 16);
+  if (small)
+    site_kernel<8><<<blocks, 256, 0, s>>>(ridges, ctr, selbits, surf_off, surf_pts, dm, VoxelDecoder::of(dm), fillmap);
+  else
+    site_kernel<16><<<blocks, 256, 0, s>>>(ridges, ctr, selbits, surf_off, surf_pts, dm, VoxelDecoder::of(dm), fillmap);
   ++*launches;
   return cudaGetLastError();
 }

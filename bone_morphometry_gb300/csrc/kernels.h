@@ -106,10 +106,11 @@ cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, c
                              const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm,
                              uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
 // Non-selected voxels on each ridge's sphere: atomic max of r2 (after the tile
-// fill).  surf_off / surf_pts: the lattice-point table covering every ridge r2.
+// fill).  surf_off / surf_pts: the lattice-point table covering every ridge r2;
+// small: 8 lanes per ridge instead of 16 (spheres of about 40 points or fewer).
 cudaError_t launch_sites(const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
-                         const uint32_t* selbits, const uint32_t* surf_off, const uint32_t* surf_pts, Dims dm,
-                         uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
+                         const uint32_t* selbits, const uint32_t* surf_off, const uint32_t* surf_pts, bool small,
+                         Dims dm, uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
 
 // Exact moment sums of f32(raw * scale) over the finite positive raw values.
 cudaError_t launch_moments(const float* map, long long n, float scale, StatsAccum* acc, cudaStream_t s,
