@@ -1,8 +1,8 @@
 """CPU oracle for the Tb.Th / Tb.Sp hot path -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
-``bench.py`` import this package, and only as the checker or the timed CPU
-baseline.  The product library (``bone_morphometry_gb300``) never imports it
+``bench.py`` import this package, and only as the reference results to compare
+against or the timed CPU baseline.  The product library (``bone_morphometry_gb300``) never imports it
 and has no CPU fallback.
 
 The C++ restatement in ``bm_oracle.cpp`` follows the reference line by line

@@ -1,7 +1,7 @@
 // CPU oracle for the Tb.Th / Tb.Sp hot path of bone-morphometry v0.7.0-rc.3.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker that the GPU library is
-// compared against, and the CPU baseline that bench.py times beside it.  It is
+// TEST INFRASTRUCTURE ONLY.  The GPU library's results are compared against
+// this file's, and bench.py times it as the CPU baseline.  It is
 // never linked into, loaded by, or called from the product library
 // (bone_morphometry_gb300/csrc), which has no CPU fallback.
 //
