@@ -74,6 +74,8 @@ def lib() -> ctypes.CDLL:
         L.orc_nonzero_stats.restype = ctypes.c_int
         L.orc_quantiles.argtypes = [f32p, sz, ctypes.c_double, f64p, sz, f64p]
         L.orc_quantiles.restype = ctypes.c_int
+        L.orc_exact_moment_sums.argtypes = [f32p, sz, ctypes.c_double, u64p, u64p, f64p]
+        L.orc_exact_moment_sums.restype = ctypes.c_uint64
         _LIB = L
     return _LIB
 
@@ -226,6 +228,31 @@ def quantiles(values: np.ndarray, scale: float, qs=(0.5, 0.1, 0.25, 0.75, 0.9)):
 def exact_moment_sums(values: np.ndarray, scale: float):
     """Exact sum and sum of squares of v = f32(raw * f32(scale)) over finite raw > 0,
     each correctly rounded to f64, plus count and max.
+
+    The per-exponent integer sums come from the C++ oracle (OpenMP, no
+    temporaries, so it serves 1024^3 maps); they are combined here in Python
+    ints.  ``exact_moment_sums_numpy`` computes the same with numpy alone.
+    """
+    raw = np.ascontiguousarray(values, np.float32).ravel()
+    s1 = np.zeros(256, np.uint64)
+    s2 = np.zeros(512, np.uint64)
+    mx = ctypes.c_double(0.0)
+    n = int(lib().orc_exact_moment_sums(_p(raw, ctypes.c_float), raw.size, float(scale), _p(s1, ctypes.c_uint64),
+                                        _p(s2, ctypes.c_uint64), ctypes.byref(mx)))
+    if n == 0:
+        raise OracleError("cannot compute statistics because the selected phase is empty")
+    total = 0
+    total_sq = 0
+    for e in range(256):
+        if s1[e]:
+            total += int(s1[e]) << e                                     # sum * 2**150
+            total_sq += ((int(s2[2 * e + 1]) << 64) | int(s2[2 * e])) << (2 * e)  # sum_sq * 2**300
+    return n, _int_ratio_to_f64(total, 150), _int_ratio_to_f64(total_sq, 300), float(mx.value)
+
+
+def exact_moment_sums_numpy(values: np.ndarray, scale: float):
+    """``exact_moment_sums`` in numpy and Python ints alone (an independent
+    check of the C++ bins; memory grows with the map, so for small maps).
 
     Every v is an f32, so v = m * 2**e with an integer 24-bit m; v*v = m*m * 2**(2e)
     is exact.  Integer sums per exponent are exact in Python ints.

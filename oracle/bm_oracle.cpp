@@ -470,6 +470,62 @@ int orc_nonzero_stats(const float* values, size_t n, double scale, double* out) 
   return 0;
 }
 
+// Exact moment sums of v = f32(raw * f32(scale)) over the finite positive raw
+// values (the terms nonzero_stats adds, metrics.rs:215-226), kept per f32
+// exponent so that no rounding happens: v = m * 2^(e - 150) with an integer
+// m < 2^24, so v*v = m*m * 2^(2e - 300).  s1[e] = sum of m (u64: < 2^24 *
+// 2^38 terms), s2[2e], s2[2e+1] = low and high 64 bits of the 128-bit sum of
+// m*m.  Returns the count of values; max_out = the largest v.  The caller
+// combines the bins with exact integer arithmetic.  Not a reference function:
+// a checker of the GPU's exactly rounded sums.
+uint64_t orc_exact_moment_sums(const float* values, size_t n, double scale, uint64_t* s1, uint64_t* s2,
+                               double* max_out) {
+  const float sf = (float)scale;
+  uint64_t count = 0;
+  float mx = 0.0f;
+  for (int e = 0; e < 256; ++e) {
+    s1[e] = 0;
+    s2[2 * e] = s2[2 * e + 1] = 0;
+  }
+#pragma omp parallel
+  {
+    uint64_t a1[256] = {};
+    unsigned __int128 a2[256] = {};
+    uint64_t c = 0;
+    float m = 0.0f;
+#pragma omp for schedule(static) nowait
+    for (long i = 0; i < (long)n; ++i) {
+      const float raw = values[i];
+      if (!std::isfinite(raw) || raw <= 0.0f) continue;
+      const float v = raw * sf;
+      uint32_t bits;
+      std::memcpy(&bits, &v, 4);
+      uint32_t e = (bits >> 23) & 0xFFu;
+      uint64_t mant = bits & 0x7FFFFFu;
+      if (e) mant |= 1u << 23;
+      else e = 1;
+      a1[e] += mant;
+      a2[e] += (unsigned __int128)(mant * mant);
+      ++c;
+      m = std::max(m, v);
+    }
+#pragma omp critical
+    {
+      for (int e = 0; e < 256; ++e) {
+        s1[e] += a1[e];
+        unsigned __int128 t = ((unsigned __int128)s2[2 * e + 1] << 64) | s2[2 * e];
+        t += a2[e];
+        s2[2 * e] = (uint64_t)t;
+        s2[2 * e + 1] = (uint64_t)(t >> 64);
+      }
+      count += c;
+      mx = std::max(mx, m);
+    }
+  }
+  *max_out = (double)mx;
+  return count;
+}
+
 // linear_quantile_unstable over the finite positive values (metrics.rs:242-298).
 // quantiles[i] in [0, 1]; out[i] = ((lower + frac*(upper-lower)) as f32 * scale_f32) as f64.
 int orc_quantiles(const float* values, size_t n, double scale, const double* quantiles, size_t nq,

@@ -134,3 +134,16 @@ def test_exact_sums_match_fsum():
     assert s == math.fsum(v.astype(np.float64))
     assert ss == math.fsum((v.astype(np.float64)) ** 2)
     assert mx == float(v.max())
+
+
+@pytest.mark.parametrize("scale", [19.5, 1e-39, 3e-38, 7.5e33, 0.37])
+def test_exact_sums_c_bins_match_numpy(scale):
+    """The C++ per-exponent bins (used on 1024^3 maps) against the numpy sums,
+    at spacings that make values subnormal, tiny or huge."""
+    rng = np.random.default_rng(11)
+    vals = (rng.random(200_000) * 300).astype(np.float32)
+    vals[::5] = 0
+    vals[3] = np.inf
+    vals[4] = -2.0
+    vals[5] = np.nan
+    assert O.exact_moment_sums(vals, scale) == O.exact_moment_sums_numpy(vals, scale)
