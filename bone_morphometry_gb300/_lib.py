@@ -133,6 +133,7 @@ SIGNATURES = {
     "bm_footprint_bytes": (ctypes.c_uint64, [_sz, _sz, _sz]),
     "bm_ctx_set_concurrent_phases": (_i, [_vp, _i]),
     "bm_ctx_set_site_method": (_i, [_vp, _i]),
+    "bm_ctx_set_wait_cycles": (_i, [_vp, ctypes.c_longlong]),
     "bm_tiff_read": (_i, [ctypes.c_char_p, ctypes.c_uint, _i, _vp, _sz, ctypes.POINTER(_sz), ctypes.POINTER(_sz),
                           ctypes.POINTER(_sz)]),
 }
@@ -220,6 +221,11 @@ class Context:
         """How the fill finds the non-selected voxels ridge spheres reach:
         BM_SITES_AUTO (0), BM_SITES_SPHERES (1) or BM_SITES_CHAINS (2)."""
         self.call("bm_ctx_set_site_method", int(method))
+
+    def set_wait_cycles(self, cycles: int = -1) -> None:
+        """Cycle limit of the device-side bounded waits (-1: the default, ~2 s;
+        0: give up at once, to exercise the timeout path)."""
+        self.call("bm_ctx_set_wait_cycles", int(cycles))
 
     def kernel_times(self) -> dict:
         """{family: (launches, total_ms)} of the kernels timed since profile(True)."""

@@ -321,13 +321,13 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   const size_t redo_bytes = (size_t)dm.w * (dm.h > dm.d ? dm.h : dm.d);
   uint8_t* redo = static_cast<uint8_t*>(ensure(ctx, ctx->redo, redo_bytes, "line flags"));
   timed(ctx, KF_EDT_Y, s, "edt y pass",
-        [&] { return launch_edt_window(1, A, B, dm, scratch, redo, ctr, s, &ctx->launches); });
+        [&] { return launch_edt_window(1, A, B, dm, scratch, redo, ctr, ctx->wait_cycles, s, &ctx->launches); });
   // local thickness keeps the x pass output (the chain passes read it): the z
   // pass then writes its own map
   uint32_t* E = d_edt ? d_edt
                       : (edt_only ? A : static_cast<uint32_t*>(ensure(ctx, ctx->edtmap, N * 4, "distance map")));
   timed(ctx, KF_EDT_Z, s, "edt z pass",
-        [&] { return launch_edt_window(2, B, E, dm, scratch, redo, ctr, s, &ctx->launches); });
+        [&] { return launch_edt_window(2, B, E, dm, scratch, redo, ctr, ctx->wait_cycles, s, &ctx->launches); });
 
   Counters hc;
   check(ctx, cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counter readback");
@@ -657,6 +657,7 @@ bm_ctx* twin_of(bm_ctx* ctx) {
   if (st != BM_OK) fail(ctx, st, "second stream context creation failed");
   t->profiling = ctx->profiling;
   t->site_method = ctx->site_method;
+  t->wait_cycles = ctx->wait_cycles;
   ctx->twin = t;
   return t;
 }
@@ -901,6 +902,14 @@ int bm_ctx_set_site_method(bm_ctx* ctx, int method) {
       fail(ctx, BM_ERR_INVALID, "site method must be 0 (auto), 1 (spheres) or 2 (chains); got %d", method);
     ctx->site_method = method;
     if (ctx->twin) ctx->twin->site_method = method;
+    return BM_OK;
+  });
+}
+
+int bm_ctx_set_wait_cycles(bm_ctx* ctx, long long cycles) {
+  return guarded(ctx, [&]() -> int {
+    ctx->wait_cycles = cycles < 0 ? -1 : cycles;
+    if (ctx->twin) ctx->twin->wait_cycles = ctx->wait_cycles;
     return BM_OK;
   });
 }

@@ -188,6 +188,7 @@ struct bm_ctx {
   cudaEvent_t inputs_ready = nullptr;
   bool split_phases = true;  // false: both phases on this context, one after the other
   int site_method = 0;       // BM_SITES_*
+  long long wait_cycles = -1;  // first-wait limit of the bounded device waits (< 0: default)
   std::mutex mu;
   std::string last_error;
   unsigned long long launches = 0;

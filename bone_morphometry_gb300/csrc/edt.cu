@@ -484,10 +484,12 @@ constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz: a copy that h
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Bounded wait for phase `parity` of the mbarrier at `bar`.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Bounded wait for phase `parity` of the mbarrier at `bar`: false once `limit`
+// cycles have passed (limit 0: gives up before the first try).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit) {
   const long long t0 = clock64();
   for (;;) {
+    if (clock64() - t0 >= limit) return false;
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -495,14 +497,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
   }
 }
 
 __global__ void __launch_bounds__(kWinThreads)
 edt_window_tma_kernel(const __grid_constant__ CUtensorMap tin, uint32_t* __restrict__ out, int axis, int n,
                       long long stride, int w, long long outer_stride, int nxt, int nchunk,
-                      uint8_t* __restrict__ redo, Counters* __restrict__ ctr, int track_max) {
+                      uint8_t* __restrict__ redo, Counters* __restrict__ ctr, int track_max, long long wait_limit) {
   __shared__ alignas(128) uint32_t buf[kTmaRows * 32];
   __shared__ alignas(8) unsigned long long bar;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -529,12 +530,13 @@ edt_window_tma_kernel(const __grid_constant__ CUtensorMap tin, uint32_t* __restr
         ::"r"(smem_u32(buf)), "l"(reinterpret_cast<unsigned long long>(&tin)), "r"(c0), "r"(c1), "r"(c2), "r"(b)
         : "memory");
   }
-  const bool landed = mbar_wait(b, 0u);
+  const bool landed = mbar_wait(b, 0u, wait_limit);
   if (!__syncthreads_and(landed)) {
-    // the copy did not complete: report it, give the copy in flight a second
-    // bounded wait (it writes into this block's shared memory) and leave
+    // the copy did not complete in time: report it, give the copy in flight a
+    // second wait with the full bound (it writes into this block's shared
+    // memory) and leave
     if (threadIdx.x == 0) atomicOr(&ctr->status, 1u);
-    mbar_wait(b, 0u);
+    mbar_wait(b, 0u, kWaitCycles);
     return;
   }
   if (q0 < kWinHalo || q0 + kWinTL + kWinHalo > n) {
@@ -715,7 +717,7 @@ bool window_map(CUtensorMap* map, const uint32_t* vol, Dims dm, int axis, unsign
 }  // namespace
 
 cudaError_t launch_edt_window(int axis, const uint32_t* in, uint32_t* out, Dims dm, void* scratch, uint8_t* redo,
-                              Counters* ctr, cudaStream_t s, unsigned long long* launches) {
+                              Counters* ctr, long long wait_cycles, cudaStream_t s, unsigned long long* launches) {
   int n;
   long long stride, outer, nlines, orows;
   if (axis == 1) {
@@ -743,7 +745,8 @@ cudaError_t launch_edt_window(int axis, const uint32_t* in, uint32_t* out, Dims 
   CUtensorMap map;
   if (axis == 1 && window_map(&map, in, dm, axis, kTmaRows)) {
     edt_window_tma_kernel<<<(unsigned)blocks, kWinThreads, 0, s>>>(map, out, axis, n, stride, dm.w, outer, nxt,
-                                                                   nchunk, redo, ctr, axis == 2 ? 1 : 0);
+                                                                   nchunk, redo, ctr, axis == 2 ? 1 : 0,
+                                                                   wait_cycles < 0 ? kWaitCycles : wait_cycles);
   } else {
     edt_window_kernel<<<(unsigned)blocks, kWinThreads, 0, s>>>(in, out, n, stride, dm.w, outer, nxt, nchunk, redo,
                                                                ctr, axis == 2 ? 1 : 0);

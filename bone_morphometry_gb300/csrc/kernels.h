@@ -35,8 +35,10 @@ cudaError_t launch_edt_line(int axis, const uint32_t* in, uint32_t* out, Dims dm
 
 // Windowed y (axis 1) / z (axis 2) pass; lines it cannot bound are recomputed
 // by the lower-envelope kernel (redo: one byte per line, scratch as above).
+// wait_cycles: limit of the TMA copy's first bounded wait (< 0: the default,
+// about 2 s); a block that gives up sets ctr->status.
 cudaError_t launch_edt_window(int axis, const uint32_t* in, uint32_t* out, Dims dm, void* scratch, uint8_t* redo,
-                              Counters* ctr, cudaStream_t s, unsigned long long* launches);
+                              Counters* ctr, long long wait_cycles, cudaStream_t s, unsigned long long* launches);
 
 // Search-template table entries lut[r2] for r2 in [lo, hi]:
 // {scan_cube(1,0,0), scan_cube(1,1,0), scan_cube(1,1,1), f32 bits of 2*sqrt(r2)}.

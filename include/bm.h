@@ -3,9 +3,9 @@
  *
  * This is the drop-in boundary for the trabecular thickness / separation
  * path of bone-morphometry v0.7.0-rc.3 (Rust).  Every entry point is plain C:
- * pointers, sizes and status codes, no CUDA or C++ types.  A Rust binding
- * (extern "C" block + the two module functions re-implemented on top of it)
- * is shown in INTEGRATION.md.
+ * pointers, sizes and status codes, no CUDA or C++ types.  A Rust caller
+ * binds it with an extern "C" block and re-implements the two module
+ * functions (edt.rs:57-60, local_thickness.rs:16) on top of it.
  *
  * Volumes use the reference layout (volume.rs:44-46): index = (z*height + y)*width + x,
  * x fastest, one byte per voxel.  Host-pointer entry points copy inputs to the
@@ -174,9 +174,12 @@ int bm_tbth_tbsp_device(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi
  * they do not control).  Takes no context; all scratch lives in one static
  * device array of 32 MiB held by every GPU that loads the library until the
  * process exits, so volumes of up to about 2.7 million voxels (128^3 fits)
- * are accepted and larger ones rejected with BM_ERR_DIMS.  The first call on
- * a device looks up the array's address (once per device, that device
- * current): make it before any stream capture.  All calls share the array and
+ * are accepted and larger ones rejected with BM_ERR_DIMS.  Every call looks
+ * up the array's device address on the current device (cudaGetSymbolAddress,
+ * which allocates nothing), so the address stays right after a
+ * cudaDeviceReset; the first call on a device also loads the library's device
+ * code there (lazy module loading): make it before any stream capture.  All
+ * calls share the array and
  * leave their data in it (the counters that must start at zero are cleared on
  * each call); calls that overlap on the GPU race and must be serialised by the
  * caller.  stream NULL = the legacy default stream; the call returns after
@@ -282,6 +285,14 @@ int bm_ctx_set_concurrent_phases(bm_ctx* ctx, int on);
  * identical either way. */
 enum { BM_SITES_AUTO = 0, BM_SITES_SPHERES = 1, BM_SITES_CHAINS = 2 };
 int bm_ctx_set_site_method(bm_ctx* ctx, int method);
+
+/* Cycle limit of the device-side bounded waits of this context's kernels (the
+ * TMA-staged y pass waits on its copy's mbarrier): cycles < 0 restores the
+ * default (4e9 cycles, about 2 s); 0 makes every first wait give up at once,
+ * which exercises the timeout path without a fault: the block records the
+ * timeout, waits (with the default bound) for its copy in flight, and the
+ * call returns BM_ERR_TIMEOUT with the context still usable.  For tests. */
+int bm_ctx_set_wait_cycles(bm_ctx* ctx, long long cycles);
 
 /* Kernel launches issued by this context since creation (library kernels only). */
 uint64_t bm_ctx_launch_count(const bm_ctx* ctx);
