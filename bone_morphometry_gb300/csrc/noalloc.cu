@@ -16,9 +16,11 @@
 //  * scratch capacity kNoAllocScratchBytes = 32 MiB: volumes of up to about
 //    2.7 million voxels (128^3 fits); larger volumes are rejected with
 //    BM_ERR_DIMS before anything is launched;
-//  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current); make
-//    that first call before any stream capture;
+//  * every call looks up the array's device address on the current device
+//    with cudaGetSymbolAddress (which allocates nothing), so a
+//    cudaDeviceReset between calls cannot leave a stale address behind; the
+//    first call on a device also loads the library's device code there (lazy
+//    module loading), so make that first call before any stream capture;
 //  * every call on a device uses the same array and leaves its contents
 //    behind; the counters that must start at zero are cleared with
 //    cudaMemsetAsync on each call; calls whose work overlaps on the GPU (other
@@ -27,7 +29,6 @@
 //  * no cudaMalloc, cudaFree or allocating library routine is called.
 #include <cstdarg>
 #include <cstdio>
-#include <mutex>
 
 #include "kernels.h"
 
@@ -38,27 +39,18 @@ void set_thread_error(const char* msg);  // api.cu: message for bm_last_error(NU
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = 32u << 20;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-std::mutex g_setup_mu;
-void* g_scratch_addr[kMaxDevices] = {};
-
-// Once per device, with that device current: the device address of the array.
+// The device address of the array on the current device.  Looked up on every
+// call rather than cached: the lookup allocates nothing, and an address kept
+// from before a cudaDeviceReset would point into a context that no longer
+// exists.
 cudaError_t scratch_for_current_device(void** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = p;
-  }
-  *out = g_scratch_addr[dev];
+  *out = p;
   return cudaSuccess;
 }
 

@@ -6,7 +6,7 @@ embedding whose allocator they do not control -- use this variant: its scratch
 is a static 32 MiB device array instead of context buffers.  These tests call
 it through the C ABI and check it against the existing entry point
 (bm_edt_sq_device) on two calls in a row, bit for bit (integer output, so the
-tolerance is zero).  The file name makes pytest collect it last.
+tolerance is zero), and the second call's map against the CPU oracle.  The file name makes pytest collect it last.
 """
 
 import ctypes
@@ -14,6 +14,7 @@ import ctypes
 import numpy as np
 import pytest
 
+import oracle as O
 from bone_morphometry_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
@@ -54,6 +55,8 @@ def test_noalloc_matches_existing_entry_point_two_calls(gpu_ctx):
         ref = _existing_edt(gpu_ctx, vol, phase)
         torch.cuda.synchronize()
         assert torch.equal(out, ref)
+    # the second call's map also against the oracle directly
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), O.edt_sq(vol.cpu().numpy(), phase))
 
 
 def test_noalloc_rejects_oversized_volume():
