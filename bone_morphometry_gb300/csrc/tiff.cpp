@@ -334,178 +334,255 @@ done:
   if (o < cap) throw TiffError{BM_ERR_INVALID, "LZW data too short for the strip"};
 }
 
-// Inflate (RFC 1950 zlib wrapper around RFC 1951 deflate data), canonical
-// Huffman decoding with per-length counts.
-class Inflater {
+// Deflate decoding (RFC 1950 zlib framing around RFC 1951 data).
+//
+// Design: each prefix code is expanded into a two-level lookup table.  The
+// root level is indexed by the next `root` input bits (9 for literals and
+// lengths, 6 for distances, 7 for the code-length code); codes no longer than
+// that fill every root slot they prefix, and each longer code's first `root`
+// bits select a root slot that links to a second-level table sized for the
+// longest code sharing that prefix.  A symbol therefore costs one or two table
+// reads and one bit-buffer shift, and building a dynamic block's tables
+// writes a few hundred slots.  Deflate sends Huffman codes most significant
+// bit first inside an LSB-first bit stream, so a code is stored reversed.
+// The length and distance symbols' base values are derived from their
+// extra-bit counts (RFC 1951 3.2.5: each base is the previous base plus the
+// span of the previous symbol's extra bits).
+class DeflateStream {
  public:
-  Inflater(const uint8_t* in, size_t n, uint8_t* out, size_t cap) : in_(in), n_(n), out_(out), cap_(cap) {}
+  DeflateStream(const uint8_t* src, size_t src_len, uint8_t* dst, size_t dst_len)
+      : src_(src), src_len_(src_len), dst_(dst), dst_len_(dst_len) {}
 
-  void run() {
-    if (n_ < 2) fail("zlib stream too short");
-    const unsigned cmf = in_[0], flg = in_[1];
-    if ((cmf & 15) != 8 || ((cmf << 8) | flg) % 31 != 0 || (flg & 32)) fail("bad zlib header");
-    pos_ = 2;
-    int last;
-    do {
-      last = getbits(1);
-      const int type = getbits(2);
-      if (type == 0) stored();
-      else if (type == 1) fixed();
-      else if (type == 2) dynamic();
-      else fail("invalid deflate block type");
-    } while (!last && o_ < cap_);
-    if (o_ < cap_) fail("deflate data too short for the strip");
+  // Decodes until the destination is full; fails on malformed data or when
+  // the stream ends first.
+  void decode_all() {
+    if (src_len_ < 2) bad("zlib stream too short");
+    const unsigned cmf = src_[0], flg = src_[1];
+    // method 8 (deflate), header checksum, and no preset dictionary
+    if ((cmf & 15u) != 8u || ((cmf << 8) | flg) % 31u != 0u || (flg & 32u)) bad("bad zlib header");
+    next_byte_ = 2;
+    bool final_block = false;
+    while (!final_block && produced_ < dst_len_) {
+      final_block = take(1) != 0;
+      switch (take(2)) {
+        case 0: raw_block(); break;
+        case 1: fixed_tables(); inflate_block(); break;
+        case 2: dynamic_tables(); inflate_block(); break;
+        default: bad("invalid deflate block type");
+      }
+    }
+    if (produced_ < dst_len_) bad("deflate data too short for the strip");
   }
 
  private:
-  struct Huff {
-    uint16_t count[16];
-    uint16_t symbol[320];
+  static constexpr int kMaxBits = 15;
+
+  // Slot encoding: bit 31 set = link {second-level offset in bits 8..30,
+  // its index width in bits 0..7}; otherwise a leaf {symbol in bits 8..30,
+  // code bits consumed at this level in bits 0..7}; 0 = no code.
+  struct Table {
+    int root = 0;
+    std::vector<uint32_t> slot;
+
+    void assign(const uint8_t* len, int nsym, int root_bits) {
+      root = root_bits;
+      int per_len[kMaxBits + 1] = {0};
+      for (int i = 0; i < nsym; ++i) per_len[len[i]]++;
+      per_len[0] = 0;
+      // canonical code assignment (RFC 1951 3.2.2): shorter codes first, then by symbol
+      unsigned next_code[kMaxBits + 1] = {0};
+      unsigned c = 0;
+      long space = 1;  // Kraft check in units of 2^-l
+      for (int l = 1; l <= kMaxBits; ++l) {
+        c = (c + (unsigned)per_len[l - 1]) << 1;
+        next_code[l] = c;
+        space = (space << 1) - per_len[l];
+        if (space < 0) throw TiffError{BM_ERR_INVALID, "over-subscribed deflate code"};
+      }
+      std::vector<uint32_t> rev(nsym, 0);
+      for (int sym = 0; sym < nsym; ++sym) {
+        const int l = len[sym];
+        if (!l) continue;
+        const unsigned code = next_code[l]++;
+        unsigned r = 0;
+        for (int b = 0; b < l; ++b) r |= ((code >> b) & 1u) << (l - 1 - b);
+        rev[sym] = r;
+      }
+      const uint32_t rmask = (1u << root) - 1u;
+      slot.assign((size_t)1 << root, 0u);
+      // second-level widths per root prefix, then their offsets
+      std::vector<uint8_t> width((size_t)1 << root, 0);
+      for (int sym = 0; sym < nsym; ++sym)
+        if (len[sym] > root) {
+          const uint32_t p = rev[sym] & rmask;
+          width[p] = (uint8_t)std::max<int>(width[p], len[sym] - root);
+        }
+      for (uint32_t p = 0; p <= rmask; ++p)
+        if (width[p]) {
+          slot[p] = 0x80000000u | ((uint32_t)slot.size() << 8) | width[p];
+          slot.resize(slot.size() + ((size_t)1 << width[p]), 0u);
+        }
+      for (int sym = 0; sym < nsym; ++sym) {
+        const int l = len[sym];
+        if (!l) continue;
+        if (l <= root) {
+          for (uint32_t k = rev[sym]; k <= rmask; k += 1u << l) slot[k] = ((uint32_t)sym << 8) | (uint32_t)l;
+        } else {
+          const uint32_t link = slot[rev[sym] & rmask];
+          const uint32_t base = (link & 0x7fffffffu) >> 8, w = link & 0xffu;
+          const uint32_t sub = l - root;
+          for (uint32_t k = rev[sym] >> root; k < (1u << w); k += 1u << sub)
+            slot[base + k] = ((uint32_t)sym << 8) | sub;
+        }
+      }
+    }
   };
 
-  [[noreturn]] void fail(const char* m) { throw TiffError{BM_ERR_INVALID, m}; }
-
-  int getbits(int need) {
-    uint32_t v = bitbuf_;
-    while (bitcnt_ < need) {
-      if (pos_ >= n_) fail("deflate data ended early");
-      v |= (uint32_t)in_[pos_++] << bitcnt_;
-      bitcnt_ += 8;
+  // Base value and extra-bit count of the 29 length and 30 distance symbols.
+  struct Bases {
+    uint16_t len_base[29], dist_base[30];
+    uint8_t len_extra[29], dist_extra[30];
+    Bases() {
+      int b = 3;
+      for (int i = 0; i < 28; ++i) {  // 8 symbols without extra bits, then 4 per extra bit count 1..5
+        len_extra[i] = (uint8_t)(i < 8 ? 0 : i / 4 - 1);
+        len_base[i] = (uint16_t)b;
+        b += 1 << len_extra[i];
+      }
+      len_base[28] = 258;  // symbol 285
+      len_extra[28] = 0;
+      int d = 1;
+      for (int i = 0; i < 30; ++i) {  // 4 symbols without extra bits, then 2 per extra bit count 1..13
+        dist_extra[i] = (uint8_t)(i < 4 ? 0 : i / 2 - 1);
+        dist_base[i] = (uint16_t)d;
+        d += 1 << dist_extra[i];
+      }
     }
-    bitbuf_ = v >> need;
-    bitcnt_ -= need;
-    return (int)(v & ((1u << need) - 1));
+  };
+  static const Bases& bases() {
+    static const Bases b;
+    return b;
   }
 
-  void put(uint8_t b) {
-    if (o_ < cap_) out_[o_] = b;
-    ++o_;
-  }
+  [[noreturn]] void bad(const char* what) { throw TiffError{BM_ERR_INVALID, what}; }
 
-  void stored() {
-    bitbuf_ = 0;
-    bitcnt_ = 0;
-    if (pos_ + 4 > n_) fail("deflate stored block header past the end");
-    const unsigned len = in_[pos_] | (in_[pos_ + 1] << 8);
-    const unsigned nlen = in_[pos_ + 2] | (in_[pos_ + 3] << 8);
-    pos_ += 4;
-    if ((len ^ 0xffffu) != nlen) fail("deflate stored block length mismatch");
-    if (pos_ + len > n_) fail("deflate stored block past the end");
-    for (unsigned i = 0; i < len; ++i) put(in_[pos_ + i]);
-    pos_ += len;
-  }
-
-  static void build(Huff& h, const uint8_t* lengths, int n) {
-    std::memset(h.count, 0, sizeof h.count);
-    for (int i = 0; i < n; ++i) h.count[lengths[i]]++;
-    h.count[0] = 0;
-    uint16_t offs[16];
-    offs[1] = 0;
-    for (int l = 1; l < 15; ++l) offs[l + 1] = offs[l] + h.count[l];
-    for (int i = 0; i < n; ++i)
-      if (lengths[i]) h.symbol[offs[lengths[i]]++] = (uint16_t)i;
-  }
-
-  int decode(const Huff& h) {
-    int code = 0, first = 0, index = 0;
-    for (int l = 1; l < 16; ++l) {
-      code |= getbits(1);
-      const int count = h.count[l];
-      if (code - count < first) return h.symbol[index + (code - first)];
-      index += count;
-      first += count;
-      first <<= 1;
-      code <<= 1;
+  // Keeps at least `n` (<= 32) bits in the buffer; past the end of the input
+  // the buffer is padded with zero bits, and consuming a padded bit fails.
+  void fill(int n) {
+    while (have_ < n) {
+      const uint64_t byte = next_byte_ < src_len_ ? src_[next_byte_] : 0u;
+      ++next_byte_;
+      acc_ |= byte << have_;
+      have_ += 8;
     }
-    fail("invalid Huffman code");
+  }
+  void drop(int n) {
+    acc_ >>= n;
+    have_ -= n;
+    if (next_byte_ > src_len_ && (next_byte_ - src_len_) * 8 > (size_t)have_) bad("deflate data ended early");
+  }
+  unsigned take(int n) {
+    if (n == 0) return 0;
+    fill(n);
+    const unsigned v = (unsigned)(acc_ & ((1ull << n) - 1));
+    drop(n);
+    return v;
+  }
+  int symbol(const Table& t) {
+    fill(kMaxBits);
+    uint32_t e = t.slot[acc_ & ((1u << t.root) - 1u)];
+    if (e & 0x80000000u) {
+      drop(t.root);
+      e = t.slot[((e & 0x7fffffffu) >> 8) + (acc_ & ((1u << (e & 0xffu)) - 1u))];
+    }
+    if (!e) bad("invalid Huffman code");
+    drop((int)(e & 0xffu));
+    return (int)(e >> 8);
   }
 
-  void codes(const Huff& lencode, const Huff& distcode) {
-    static const uint16_t lbase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27,
-                                       31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
-    static const uint8_t lext[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
-                                     2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
-    static const uint16_t dbase[30] = {1,    2,    3,    4,    5,    7,     9,     13,    17,    25,
-                                       33,   49,   65,   97,   129,  193,   257,   385,   513,   769,
-                                       1025, 1537, 2049, 3073, 4097, 6145,  8193,  12289, 16385, 24577};
-    static const uint8_t dext[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
-                                     6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+  void emit(uint8_t b) { dst_[produced_++] = b; }
+
+  void raw_block() {
+    drop(have_ & 7);  // to the byte boundary
+    const unsigned len = take(16), inv = take(16);
+    if ((len ^ 0xffffu) != inv) bad("deflate stored block length mismatch");
+    for (unsigned i = 0; i < len && produced_ < dst_len_; ++i) emit((uint8_t)take(8));
+  }
+
+  void fixed_tables() {
+    uint8_t len[288];
+    for (int i = 0; i < 288; ++i) len[i] = i < 144 ? 8 : i < 256 ? 9 : i < 280 ? 7 : 8;
+    lit_.assign(len, 288, 9);
+    uint8_t dl[30];
+    std::memset(dl, 5, sizeof dl);
+    dist_.assign(dl, 30, 6);
+  }
+
+  void dynamic_tables() {
+    const int nlit = (int)take(5) + 257, ndist = (int)take(5) + 1, nclen = (int)take(4) + 4;
+    if (nlit > 286 || ndist > 30) bad("bad deflate code counts");
+    // code-length alphabet, its lengths sent in this order (RFC 1951 3.2.7)
+    static const uint8_t kClenOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+    uint8_t clen[19] = {0};
+    for (int i = 0; i < nclen; ++i) clen[kClenOrder[i]] = (uint8_t)take(3);
+    Table meta;
+    meta.assign(clen, 19, 7);
+    uint8_t len[286 + 30] = {0};
+    const int total = nlit + ndist;
+    int k = 0;
+    while (k < total) {
+      const int c = symbol(meta);
+      int run = 1;
+      uint8_t v = (uint8_t)c;
+      if (c == 16) {
+        if (k == 0) bad("deflate repeat with no previous length");
+        v = len[k - 1];
+        run = 3 + (int)take(2);
+      } else if (c == 17) {
+        v = 0;
+        run = 3 + (int)take(3);
+      } else if (c == 18) {
+        v = 0;
+        run = 11 + (int)take(7);
+      }
+      if (k + run > total) bad("deflate code lengths overflow");
+      std::memset(len + k, v, (size_t)run);
+      k += run;
+    }
+    if (len[256] == 0) bad("deflate block without an end-of-block code");
+    lit_.assign(len, nlit, 9);
+    dist_.assign(len + nlit, ndist, 6);
+  }
+
+  void inflate_block() {
+    const Bases& B = bases();
     for (;;) {
-      int sym = decode(lencode);
-      if (sym < 256) {
-        put((uint8_t)sym);
-      } else if (sym == 256) {
-        return;
-      } else {
-        sym -= 257;
-        if (sym >= 29) fail("invalid deflate length symbol");
-        const int len = lbase[sym] + getbits(lext[sym]);
-        const int ds = decode(distcode);
-        if (ds >= 30) fail("invalid deflate distance symbol");
-        const size_t dist = dbase[ds] + getbits(dext[ds]);
-        if (dist > o_) fail("deflate distance before the start of the data");
-        for (int i = 0; i < len; ++i) {
-          const size_t from = o_ - dist;
-          put(from < cap_ ? out_[from] : 0);
-        }
+      const int c = symbol(lit_);
+      if (c < 256) {
+        if (produced_ == dst_len_) return;
+        emit((uint8_t)c);
+        continue;
       }
+      if (c == 256) return;
+      const int li = c - 257;
+      if (li >= 29) bad("invalid deflate length symbol");
+      const int length = B.len_base[li] + (int)take(B.len_extra[li]);
+      const int di = symbol(dist_);
+      if (di >= 30) bad("invalid deflate distance symbol");
+      const size_t distance = B.dist_base[di] + take(B.dist_extra[di]);
+      if (distance > produced_) bad("deflate distance before the start of the data");
+      for (int i = 0; i < length && produced_ < dst_len_; ++i) emit(dst_[produced_ - distance]);
+      if (produced_ == dst_len_) return;
     }
   }
 
-  void fixed() {
-    uint8_t l[288 + 30];
-    int i = 0;
-    for (; i < 144; ++i) l[i] = 8;
-    for (; i < 256; ++i) l[i] = 9;
-    for (; i < 280; ++i) l[i] = 7;
-    for (; i < 288; ++i) l[i] = 8;
-    Huff lc, dc;
-    build(lc, l, 288);
-    for (i = 0; i < 30; ++i) l[i] = 5;
-    build(dc, l, 30);
-    codes(lc, dc);
-  }
-
-  void dynamic() {
-    static const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
-    const int nlen = getbits(5) + 257, ndist = getbits(5) + 1, ncode = getbits(4) + 4;
-    if (nlen > 286 || ndist > 30) fail("bad deflate code counts");
-    uint8_t l[320] = {0};
-    for (int i = 0; i < ncode; ++i) l[order[i]] = (uint8_t)getbits(3);
-    Huff lc, dc;
-    build(lc, l, 19);
-    int idx = 0;
-    uint8_t lens[320] = {0};
-    while (idx < nlen + ndist) {
-      int sym = decode(lc);
-      if (sym < 16) {
-        lens[idx++] = (uint8_t)sym;
-      } else {
-        int rep = 0, val = 0;
-        if (sym == 16) {
-          if (idx == 0) fail("deflate repeat with no previous length");
-          val = lens[idx - 1];
-          rep = 3 + getbits(2);
-        } else if (sym == 17) {
-          rep = 3 + getbits(3);
-        } else {
-          rep = 11 + getbits(7);
-        }
-        if (idx + rep > nlen + ndist) fail("deflate code lengths overflow");
-        while (rep--) lens[idx++] = (uint8_t)val;
-      }
-    }
-    build(lc, lens, nlen);
-    build(dc, lens + nlen, ndist);
-    codes(lc, dc);
-  }
-
-  const uint8_t* in_;
-  size_t n_, pos_ = 0;
-  uint8_t* out_;
-  size_t cap_, o_ = 0;
-  uint32_t bitbuf_ = 0;
-  int bitcnt_ = 0;
+  const uint8_t* src_;
+  size_t src_len_, next_byte_ = 0;
+  uint8_t* dst_;
+  size_t dst_len_, produced_ = 0;
+  uint64_t acc_ = 0;
+  int have_ = 0;
+  Table lit_, dist_;
 };
 
 // Decodes one strip or tile into out (rows x row_len bytes).
@@ -519,7 +596,7 @@ void decode_chunk(const Page& pg, const uint8_t* in, size_t n, uint8_t* out, siz
     case 32773: unpackbits(in, n, out, cap); break;
     case 5: unlzw(in, n, out, cap); break;
     case 8:
-    case 32946: Inflater(in, n, out, cap).run(); break;
+    case 32946: DeflateStream(in, n, out, cap).decode_all(); break;
     default: throw TiffError{BM_ERR_INVALID, fmt("unsupported compression method %u", pg.compression)};
   }
   if (pg.predictor == 2) {

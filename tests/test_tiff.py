@@ -142,3 +142,43 @@ def test_tiff_stack_to_thickness_on_gpu(tmp_path, gpu_ctx):
     assert got.thickness.mean == ref.thickness.mean and got.spacing.mean == ref.spacing.mean
     assert got.thickness.standard_deviation == ref.thickness.standard_deviation
     assert got.spacing.maximum == ref.spacing.maximum
+
+
+@pytest.mark.parametrize("mode", sorted(T.DEFLATE_MODES))
+@pytest.mark.parametrize("kind", ["binary", "gray", "noise"])
+def test_deflate_every_block_type(tmp_path, mode, kind):
+    """Stored, fixed-code and dynamic-code Deflate blocks (zlib's strategies),
+    strips of a whole 200x300 page (several blocks each) and of 3 rows."""
+    rng = np.random.default_rng(hash((mode, kind)) & 0xFFFF)
+    if kind == "binary":
+        vol = stack(5, d=3, h=200, w=300)
+    elif kind == "gray":
+        vol = stack(6, d=3, h=200, w=300, binary=False)
+    else:
+        vol = rng.integers(0, 256, size=(3, 200, 300)).astype(np.uint8)
+    for rps in (None, 3):
+        p = tmp_path / ("d%s.tif" % rps)
+        T.write_tiff(p, list(vol), compression=T.DEFLATE, rows_per_strip=rps, deflate_mode=mode)
+        for thr in (0, 100, 200):
+            assert np.array_equal(read_binary_tiff(p, threshold=thr).array(), (vol > thr).astype(np.uint8))
+
+
+def test_corrupt_deflate_data_is_an_error(tmp_path):
+    vol = stack(8, d=2, h=64, w=64, binary=False)
+    p = tmp_path / "c.tif"
+    T.write_tiff(p, list(vol), compression=T.DEFLATE)
+    raw = bytearray(p.read_bytes())
+    rng = np.random.default_rng(3)
+    failures = 0
+    for trial in range(40):
+        bad = bytearray(raw)
+        # flip bytes inside the first strip's data (after the 8-byte header)
+        for k in rng.integers(10, 200, size=4):
+            bad[int(k)] ^= 0xA5
+        q = tmp_path / ("c%d.tif" % trial)
+        q.write_bytes(bytes(bad))
+        try:
+            read_binary_tiff(q, threshold=100)
+        except BoneMorphometryError:
+            failures += 1  # a clean error, never a crash
+    assert failures > 0

@@ -77,7 +77,19 @@ def lzw(data: bytes) -> bytes:
     return bytes(out)
 
 
-def encode(raw: bytes, compression: int) -> bytes:
+# zlib settings for Deflate data: every block type (stored, fixed and dynamic
+# codes) and several match strategies
+DEFLATE_MODES = {
+    "default": (6, zlib.Z_DEFAULT_STRATEGY),
+    "stored": (0, zlib.Z_DEFAULT_STRATEGY),
+    "fixed": (6, zlib.Z_FIXED),
+    "huffman": (6, zlib.Z_HUFFMAN_ONLY),
+    "rle": (6, zlib.Z_RLE),
+    "best": (9, zlib.Z_FILTERED),
+}
+
+
+def encode(raw: bytes, compression: int, deflate_mode: str = "default") -> bytes:
     if compression == NONE:
         return raw
     if compression == PACKBITS:
@@ -85,7 +97,9 @@ def encode(raw: bytes, compression: int) -> bytes:
     if compression == LZW:
         return lzw(raw)
     if compression == DEFLATE:
-        return zlib.compress(raw, 6)
+        level, strategy = DEFLATE_MODES[deflate_mode]
+        c = zlib.compressobj(level, zlib.DEFLATED, 15, 9, strategy)
+        return c.compress(raw) + c.flush()
     raise ValueError(compression)
 
 
@@ -96,7 +110,7 @@ def difference(rows: np.ndarray) -> np.ndarray:
 
 
 def write_tiff(path, pages, compression=NONE, big=False, byteorder="<", rows_per_strip=None, tile=None,
-               predictor=1, bits=8, photometric=1, samples=1, sample_format=1):
+               predictor=1, bits=8, photometric=1, samples=1, sample_format=1, deflate_mode="default"):
     """pages: list of 2-D u8 (or u16 when bits == 16) arrays, one per page."""
     e = byteorder
     head = bytearray()
@@ -120,7 +134,7 @@ def write_tiff(path, pages, compression=NONE, big=False, byteorder="<", rows_per
                     t[:part.shape[0], :part.shape[1]] = part
                     if predictor == 2:
                         t = difference(t)
-                    chunks.append(encode(t.tobytes(), compression))
+                    chunks.append(encode(t.tobytes(), compression, deflate_mode))
         else:
             rps = rows_per_strip or h
             for y in range(0, h, rps):
