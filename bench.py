@@ -7,15 +7,24 @@ EDT and the local thickness of ROI-clipped bone (Tb.Th) and of in-ROI marrow
 voxels (counted once per specimen) per second.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gpu|reference]
+  python bench.py --profile-case N [--plates]
 
 --impl gpu (default): device-resident timing (``value``) with CUDA events on the
 launching stream, per-kernel event timing (roofline of the dominant kernel),
 an end-to-end leg through the host-pointer C ABI entry point with H2D/D2H in
 the timed region (``e2e``), the CPU oracle timed on a bounded sample
 (``cpu_baseline``), and nvidia-smi clock samples taken during the timed region.
+At N = 1 the extras add the 1024^3 plate specimen (the same legs), the
+64-specimen batch and the Poisson serving runs.
 --impl reference: the reference algorithm's CPU implementation (the C++
 oracle, OpenMP over all host cores; the Rust reference cannot be built here)
-on bounded samples of the same workload.
+on the whole specimen of the workload, every step.
+--profile-case N: a small case for profilers with a kernel filter (no timing):
+one Tb.Th local thickness of a seeded N^3 specimen as warm-up (tables built),
+then Tb.Th and Tb.Sp again -- the launches worth capturing.  The specimen is
+the 512^3 workload's generator at edge N (sigma 5, BV/TV 0.15, cylinder ROI of
+radius 0.47 N); with --plates the 1024^3 workload's (sigma (4, 4, 8), BV/TV
+0.30, sphere ROI of radius 500 N / 1024).
 
 Multi-process (torchrun): every rank processes its own specimen (different
 seed, same shape) with no data exchange -- replicas, weak scaling; rank 0
@@ -80,7 +89,11 @@ def parse_args(argv=None):
     ap.add_argument("--serve-rate-light", type=float, default=80.0,
                     help="second Poisson rate, below the GPU's capacity for the mix (0: skip)")
     ap.add_argument("--cpu-sample-slices", type=int, default=0,
-                    help="z-slab depth of the CPU sample (default: sized to ~10 s)")
+                    help="z-slab depth of the GPU arm's CPU-baseline sample (default: sized to ~10 s)")
+    ap.add_argument("--extra-steps", type=int, default=5, help="timed steps of the 1024^3 extra leg")
+    ap.add_argument("--profile-case", type=int, default=0, metavar="N",
+                    help="run the profiling case at edge N instead of the benchmark")
+    ap.add_argument("--plates", action="store_true", help="profiling case with the 1024^3 plate generator")
     return ap.parse_args(argv)
 
 
@@ -176,17 +189,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_sample_run(sp, slices: int, threads: int):
-    """Both phases of the oracle on a z-slab of the specimen; returns (voxels, seconds)."""
+def cpu_run(sp, z0: int, slices: int, threads: int):
+    """Both phases of the oracle (the reference algorithm) on z-slices
+    [z0, z0 + slices) of the specimen -- the whole specimen when they cover it;
+    returns (voxels, seconds)."""
     import numpy as np
 
     import oracle as O
 
     if threads:
         O.set_threads(threads)
-    z0 = max(0, sp.bone.shape[0] // 2 - slices // 2)
-    bone = np.ascontiguousarray(sp.bone[z0:z0 + slices])
-    roi = np.ascontiguousarray(sp.roi[z0:z0 + slices])
+    d = sp.bone.shape[0]
+    whole = z0 == 0 and slices >= d
+    bone = sp.bone if whole else np.ascontiguousarray(sp.bone[z0:z0 + slices])
+    roi = sp.roi if whole else np.ascontiguousarray(sp.roi[z0:z0 + slices])
     t0 = time.perf_counter()
     for sel in (True, False):
         m = O.phase_inside(bone, roi, sel)
@@ -202,37 +218,50 @@ def default_slices(sp):
     return max(4, min(d, int(target_vox / (h * w))))
 
 
+def workload_config(workload: str, shape, world: int) -> dict:
+    """The ``config`` object of the JSON line (the same for both arms)."""
+    d, h, w = shape
+    n_vox = d * h * w
+    return {"workload": "%s: %s" % (workload, WORKLOADS[workload]["desc"]),
+            "shape_whd": [w, h, d], "voxels_per_specimen": n_vox, "phases": ["Tb.Th", "Tb.Sp"],
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "inputs (%d MiB) and u32 maps (%d MiB each) larger than the 129 MB L2"
+                  % (2 * n_vox >> 20, 4 * n_vox >> 20)}
+
+
 def run_reference(args, rank, world):
-    """CPU implementation of the reference algorithm (oracle port), all host threads."""
+    """CPU implementation of the reference algorithm (oracle port), all host
+    threads, on the whole specimen of the workload every step (metrics.rs:97-121:
+    both phases' local thickness and statistics)."""
     import oracle as O
 
     if rank != 0:
         return 0
     sp = make_specimen(args.workload, 0)
-    slices = args.cpu_sample_slices or default_slices(sp)
+    d, h, w = sp.bone.shape
     threads = os.cpu_count() or 1
     O.set_threads(threads)
     for _ in range(max(0, args.warmup)):
-        cpu_sample_run(sp, slices, threads)
+        cpu_run(sp, 0, d, threads)
     times = []
     vox = 0
     for _ in range(args.steps):
-        vox, dt = cpu_sample_run(sp, slices, threads)
+        vox, dt = cpu_run(sp, 0, d, threads)
         times.append(dt)
     total = sum(times)
     value = vox * len(times) / total / 1e9
-    d, h, w = sp.bone.shape
-    sample = "z-slab %dx%dx%d of the %s specimen, both phases" % (w, h, slices, args.workload)
+    sample = "the whole %dx%dx%d %s specimen every step, both phases" % (w, h, d, args.workload)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u32/f32",
-        "data": "synthetic", "config": {"workload": "%s: %s" % (args.workload, WORKLOADS[args.workload]["desc"]),
-                                        "sample": sample},
+        "data": "synthetic (seeded Gaussian-smoothed noise, thresholded; no public dataset)",
+        "config": workload_config(args.workload, sp.bone.shape, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the Rust reference cannot be built here (no cargo/rustc); the timed CPU path is the C++ "
-                "restatement of edt.rs / local_thickness.rs / metrics.rs with OpenMP in place of rayon",
+                "restatement of edt.rs / local_thickness.rs / metrics.rs with OpenMP in place of rayon "
+                "(serial where the reference is serial)",
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -409,11 +438,130 @@ def bench_serving(n_requests=64, rate=200.0, budget=120e9, workers=(2, 4)):
             "data": "torch GPU generator, edges log-uniform [64,768]; host-pointer requests (H2D inside)"}
 
 
-def run_gpu(args, rank, world, local):
-    import numpy as np
+def measure_specimen(ctx, sp, steps: int, warmup: int, local: int, barrier, reduce_max):
+    """Device-resident timing, per-kernel event timing and the end-to-end leg
+    of one specimen (both phases, metrics.rs:97-121) on one context."""
     import torch
 
-    from bone_morphometry_gb300 import Context, analyze_thickness
+    from bone_morphometry_gb300 import analyze_thickness
+
+    n_vox = sp.bone.size
+    stream = torch.cuda.current_stream()
+    bone = torch.from_numpy(sp.bone).cuda()
+    roi = torch.from_numpy(sp.roi).cuda()
+    for _ in range(max(3, warmup)):
+        ref_res = analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
+    torch.cuda.synchronize()
+
+    # -- device-resident leg (Tb.Th and Tb.Sp side by side, the library default) ---------------
+    launches0 = ctx.launches
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(steps):
+            res = analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = ctx.launches - launches0
+    ms = reduce_max(ev0.elapsed_time(ev1) / steps)
+    assert res.thickness.mean == ref_res.thickness.mean and res.spacing.mean == ref_res.spacing.mean
+    # -- per-kernel times for the roofline: the phases one after the other, so that
+    # every kernel has the GPU to itself; CUDA events on each launch's stream ----------------
+    ctx.set_concurrent_phases(False)
+    ctx.profile(True)
+    for _ in range(steps):
+        analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
+    torch.cuda.synchronize()
+    ktimes = ctx.kernel_times()
+    ctx.profile(False)
+    ctx.set_concurrent_phases(True)
+    del bone, roi
+
+    # -- end-to-end leg through the host-pointer entry point (pinned host inputs) --------------
+    hb = torch.empty(sp.bone.shape, dtype=torch.uint8, pin_memory=True)
+    hr = torch.empty(sp.roi.shape, dtype=torch.uint8, pin_memory=True)
+    hb.numpy()[:] = sp.bone
+    hr.numpy()[:] = sp.roi
+    hbn, hrn = hb.numpy(), hr.numpy()
+    analyze_thickness(hbn, hrn, sp.spacing_um, ctx=ctx)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        res_e = analyze_thickness(hbn, hrn, sp.spacing_um, ctx=ctx)
+    e2e_s = (time.perf_counter() - t0) / steps
+    assert res_e.thickness.mean == ref_res.thickness.mean
+    e2e_s = reduce_max(e2e_s)
+    del hb, hr, hbn, hrn
+    return {"ms": ms, "e2e_s": e2e_s, "ktimes": ktimes, "clocks": clk.summary(), "launches": launches,
+            "result": res}
+
+
+def kernel_report(ktimes, n_vox: int, traffic: dict):
+    """(kernels, roofline of the dominant kernel, EDT roofline) from the profiler's families."""
+    total_kernel_ms = sum(v[1] for v in ktimes.values()) or 1.0
+    kernels = {}
+    for name, (nl, tms) in ktimes.items():
+        if nl == 0:
+            continue
+        kernels[name] = {"launches": nl, "ms_per_launch": tms / nl, "share": tms / total_kernel_ms}
+    peak, peak_src = measured_peak_gbs()
+
+    def roof(name):
+        nl, tms = ktimes[name]
+        bpl = ALGO_BYTES_PER_VOXEL[name] * n_vox
+        achieved = bpl / (tms / nl * 1e-3) / 1e9
+        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic.get(name), "algorithmic_bytes": bpl,
+                "peak_source": peak_src}
+
+    dominant = max((k for k in ktimes if ktimes[k][0] and ALGO_BYTES_PER_VOXEL.get(k, 0) > 0),
+                   key=lambda k: ktimes[k][1])
+    edt_ms = sum(ktimes[k][1] for k in EDT_FAMILIES) / max(1, ktimes["edt_x"][0])
+    edt_bytes = sum(ALGO_BYTES_PER_VOXEL[k] for k in EDT_FAMILIES) * n_vox
+    edt_achieved = edt_bytes / (edt_ms * 1e-3) / 1e9
+    edt_roof = {"bound": "hbm", "achieved": edt_achieved, "peak": peak, "unit": "GB/s", "frac": edt_achieved / peak,
+                "algorithmic_bytes_per_phase": edt_bytes, "ms_per_phase": edt_ms, "peak_source": peak_src}
+    return kernels, roof(dominant), edt_roof
+
+
+def bench_single1024(args, local):
+    """The 1024^3 plate specimen (the largest single-GPU configuration): the
+    same legs as the headline, on a context of its own."""
+    import torch
+
+    from bone_morphometry_gb300 import Context
+
+    sp = make_specimen("single1024", 0)
+    n_vox = sp.bone.size
+    ctx = Context(local)
+    try:
+        m = measure_specimen(ctx, sp, args.extra_steps, 3, local, lambda: None, lambda v: v)
+    finally:
+        ctx.close()
+        torch.cuda.empty_cache()
+    kernels, roofline, edt_roof = kernel_report(m["ktimes"], n_vox, committed_traffic().get("single1024", {}))
+    res = m["result"]
+    return {"workload": "single1024: " + WORKLOADS["single1024"]["desc"], "shape_whd": [1024, 1024, 1024],
+            "steps": args.extra_steps, "warmup": 3, "value": n_vox / (m["ms"] * 1e-3) / 1e9, "unit": UNIT,
+            "ms_per_step": m["ms"],
+            "e2e": {"value": n_vox / m["e2e_s"] / 1e9, "unit": UNIT, "h2d_bytes_per_step": 2 * n_vox,
+                    "d2h_bytes_per_step": 2 * 104, "ms_per_step": m["e2e_s"] * 1e3},
+            "gpu_launches": m["launches"], "roofline": roofline, "edt_roofline": edt_roof, "kernels": kernels,
+            "clocks": m["clocks"],
+            "result": {"TbTh_mean_um": res.thickness.mean, "TbTh_sd_um": res.thickness.standard_deviation,
+                       "TbSp_mean_um": res.spacing.mean, "TbSp_sd_um": res.spacing.standard_deviation},
+            "data": "torch GPU generator (seeded), inputs 2 GiB and maps 4 GiB each: larger than L2"}
+
+
+def run_gpu(args, rank, world, local):
+    import torch
+
+    from bone_morphometry_gb300 import Context
     from bone_morphometry_gb300.replicas import max_over_ranks
 
     torch.cuda.set_device(local)
@@ -430,99 +578,29 @@ def run_gpu(args, rank, world, local):
     sp = make_specimen(args.workload, rank)
     n_vox = sp.bone.size
     ctx = Context(local)
-    stream = torch.cuda.current_stream()
-    bone = torch.from_numpy(sp.bone).cuda()
-    roi = torch.from_numpy(sp.roi).cuda()
-
-    for _ in range(max(3, args.warmup)):
-        ref_res = analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
-    torch.cuda.synchronize()
-
-    # -- device-resident leg (Tb.Th and Tb.Sp side by side, the library default) ---------------
-    launches0 = ctx.launches
-    barrier()
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            res = analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    launches = ctx.launches - launches0
-    ms = ev0.elapsed_time(ev1) / args.steps
-    # -- per-kernel times for the roofline: the phases one after the other, so that
-    # every kernel has the GPU to itself; CUDA events on each launch's stream ----------------
-    ctx.set_concurrent_phases(False)
-    ctx.profile(True)
-    for _ in range(args.steps):
-        analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
-    torch.cuda.synchronize()
-    ktimes = ctx.kernel_times()
-    ctx.profile(False)
-    ctx.set_concurrent_phases(True)
-    assert res.thickness.mean == ref_res.thickness.mean and res.spacing.mean == ref_res.spacing.mean
-    ms = max_over_ranks(ms)
+    m = measure_specimen(ctx, sp, args.steps, args.warmup, local, barrier, max_over_ranks)
+    ms, res = m["ms"], m["result"]
     value = world * n_vox / (ms * 1e-3) / 1e9
-
-    # -- end-to-end leg through the host-pointer entry point (pinned host inputs) --------------
-    hb = torch.empty(sp.bone.shape, dtype=torch.uint8, pin_memory=True)
-    hr = torch.empty(sp.roi.shape, dtype=torch.uint8, pin_memory=True)
-    hb.numpy()[:] = sp.bone
-    hr.numpy()[:] = sp.roi
-    hbn, hrn = hb.numpy(), hr.numpy()
-    analyze_thickness(hbn, hrn, sp.spacing_um, ctx=ctx)
-    barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        res_e = analyze_thickness(hbn, hrn, sp.spacing_um, ctx=ctx)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    assert res_e.thickness.mean == ref_res.thickness.mean
-    e2e_s = max_over_ranks(e2e_s)
-    e2e_value = world * n_vox / e2e_s / 1e9
+    e2e_value = world * n_vox / m["e2e_s"] / 1e9
 
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return 0
 
-    # -- per-kernel times and roofline -------------------------------------------------------
-    total_kernel_ms = sum(v[1] for v in ktimes.values()) or 1.0
-    kernels = {}
-    for name, (nl, tms) in ktimes.items():
-        if nl == 0:
-            continue
-        kernels[name] = {"launches": nl, "ms_per_launch": tms / nl, "share": tms / total_kernel_ms}
-    peak, peak_src = measured_peak_gbs()
-    traffic = committed_traffic().get(args.workload, {})
+    kernels, roofline, edt_roof = kernel_report(m["ktimes"], n_vox, committed_traffic().get(args.workload, {}))
 
-    def roof(name):
-        nl, tms = ktimes[name]
-        bpl = ALGO_BYTES_PER_VOXEL[name] * n_vox
-        achieved = bpl / (tms / nl * 1e-3) / 1e9
-        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic.get(name), "algorithmic_bytes": bpl,
-                "peak_source": peak_src}
-
-    dominant = max((k for k in ktimes if ktimes[k][0] and ALGO_BYTES_PER_VOXEL.get(k, 0) > 0),
-                   key=lambda k: ktimes[k][1])
-    edt_ms = sum(ktimes[k][1] for k in EDT_FAMILIES) / max(1, ktimes["edt_x"][0])
-    edt_bytes = sum(ALGO_BYTES_PER_VOXEL[k] for k in EDT_FAMILIES) * n_vox
-    edt_achieved = edt_bytes / (edt_ms * 1e-3) / 1e9
-
-    # -- CPU baseline (rank 0, N = 1 only) ------------------------------------------------------
+    # -- CPU baseline (rank 0, N = 1 only): the oracle on a bounded sample --------------------
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        slices = args.cpu_sample_slices or default_slices(sp)
-        vox, dt = cpu_sample_run(sp, slices, threads)
         d, h, w = sp.bone.shape
+        slices = args.cpu_sample_slices or default_slices(sp)
+        z0 = max(0, d // 2 - slices // 2)
+        vox, dt = cpu_run(sp, z0, slices, threads)
         # one thread too, on a slab 1/8 as thick (the same algorithm, no parallelism)
         slices1 = max(4, slices // 8)
-        vox1, dt1 = cpu_sample_run(sp, slices1, 1)
+        vox1, dt1 = cpu_run(sp, max(0, d // 2 - slices1 // 2), slices1, 1)
         cpu = {"value": vox / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "z-slab %dx%dx%d of the same specimen, both phases, %.1f s" % (w, h, slices, dt),
                "value_1_thread": vox1 / dt1 / 1e9,
@@ -530,32 +608,27 @@ def run_gpu(args, rank, world, local):
 
     extras = {}
     if world == 1 and not args.no_extras:
+        if args.workload != "single1024":
+            extras["single1024"] = bench_single1024(args, local)
         extras["batch64"] = bench_batch(ctx)
         extras["serving"] = bench_serving(args.serve_requests, args.serve_rate)
         if args.serve_rate_light > 0:
             # the same mix at a rate the GPU keeps up with: latency without a growing queue
             extras["serving_light"] = bench_serving(args.serve_requests, args.serve_rate_light)
 
-    d, h, w = sp.bone.shape
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u8/u32/f32 (integer EDT and r^2, f32 map, exact f64 stats)",
+        "vs_baseline": None, "dtype": "u8/u32/f32 (integer EDT and r^2, f32 map, f64 stats)",
         "data": "synthetic (seeded Gaussian-smoothed noise, thresholded; no public dataset)",
-        "config": {"workload": "%s: %s" % (args.workload, WORKLOADS[args.workload]["desc"]),
-                   "shape_whd": [w, h, d], "voxels_per_specimen": n_vox, "phases": ["Tb.Th", "Tb.Sp"],
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "inputs (%d MiB) and u32 maps (%d MiB each) larger than the 129 MB L2"
-                         % (2 * n_vox >> 20, 4 * n_vox >> 20)},
+        "config": workload_config(args.workload, sp.bone.shape, world),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n_vox,
-                "d2h_bytes_per_step": 2 * 104, "ms_per_step": e2e_s * 1e3},
-        "gpu_launches": launches,
-        "roofline": roof(dominant),
-        "edt_roofline": {"bound": "hbm", "achieved": edt_achieved, "peak": peak, "unit": "GB/s",
-                         "frac": edt_achieved / peak, "algorithmic_bytes_per_phase": edt_bytes,
-                         "ms_per_phase": edt_ms, "peak_source": peak_src},
+                "d2h_bytes_per_step": 2 * 104, "ms_per_step": m["e2e_s"] * 1e3},
+        "gpu_launches": m["launches"],
+        "roofline": roofline,
+        "edt_roofline": edt_roof,
         "kernels": kernels,
-        "clocks": clk.summary(),
+        "clocks": m["clocks"],
         "cpu_baseline": cpu,
         "result": {"TbTh_mean_um": res.thickness.mean, "TbTh_sd_um": res.thickness.standard_deviation,
                    "TbSp_mean_um": res.spacing.mean, "TbSp_sd_um": res.spacing.standard_deviation},
@@ -567,8 +640,36 @@ def run_gpu(args, rank, world, local):
     return 0
 
 
+def run_profile_case(args) -> int:
+    """A small case for profilers with a kernel filter (no timing, no JSON line)."""
+    import numpy as np
+    import torch
+
+    from bone_morphometry_gb300 import Context, Phase, local_thickness
+    from bone_morphometry_gb300 import synthetic as S
+
+    n = args.profile_case
+    if args.plates:
+        sp = S.make_specimen_torch((n, n, n), (4.0, 4.0, 8.0), 0.30, "sphere", 500.0 * n / 1024, 8.0, 1003,
+                                   to_host=True)
+    else:
+        sp = S.make_specimen((n, n, n), 5.0, 0.15, "cylinder", 0.47 * n, 19.5, 1002)
+    ctx = Context(0)
+    th = torch.from_numpy(((sp.roi != 0) & (sp.bone != 0)).astype(np.uint8)).cuda()
+    ma = torch.from_numpy(((sp.roi != 0) & (sp.bone == 0)).astype(np.uint8)).cuda()
+    local_thickness(th, Phase.FOREGROUND, ctx=ctx)
+    local_thickness(th, Phase.FOREGROUND, ctx=ctx)
+    local_thickness(ma, Phase.FOREGROUND, ctx=ctx)
+    torch.cuda.synchronize()
+    ctx.close()
+    print("profile case done: %d^3%s" % (n, " plates" if args.plates else ""))
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
+    if args.profile_case:
+        return run_profile_case(args)
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)

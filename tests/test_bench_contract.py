@@ -1,5 +1,5 @@
 """bench.py's host-side contract, without a GPU: the reference arm's JSON line
-(the CPU implementation timed on a bounded sample) and the helpers that shape
+(the CPU implementation timed on the whole specimen) and the helpers that shape
 the GPU arm's line (clock samples and their throttle reasons, percentiles)."""
 
 import json
@@ -28,6 +28,9 @@ def test_reference_arm_prints_one_contract_line():
                 "vs_baseline", "dtype", "data", "config"):
         assert key in d
     assert d["config"]["workload"].startswith("plain128")
+    # the same config object as the GPU arm's line: the whole specimen every step
+    assert d["config"] == bench.workload_config("plain128", (128, 128, 128), 1)
+    assert "whole" in d["cpu_baseline"]["sample"]
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
     e2e = d["e2e"]
