@@ -103,8 +103,9 @@ def run_config(gpu_ctx, config, sp):
         check_exact_stats(got, ref.thickness, sp.spacing_um)
         dev = seq_deviation(config, name, got, ref.thickness, sp.spacing_um)
         # the reference's sequential sums differ from the exact ones by its own
-        # rounding (SD amplified by mean^2 / var): recorded, bounded loosely here
-        assert dev["max_equal"] and dev["rel_mean"] <= 1e-12 and dev["rel_sd"] <= 1e-8, dev
+        # rounding (SD amplified by mean^2 / var); measured on these specimens:
+        # mean up to 6.9e-12, SD up to 4.6e-10 relative
+        assert dev["max_equal"] and dev["rel_mean"] <= 1e-10 and dev["rel_sd"] <= 1e-8, dev
         del ref, m
     del res
 
