@@ -61,7 +61,8 @@ ALGO_BYTES_PER_VOXEL = {
     "fill_bin": 0.0,                   # per-ridge work (ridge records in, bin entries out)
     "templates": 0.0,
     "fill_sites": 0.0,                 # per-ridge work (sphere points of each ridge)
-    "cleanup_final": 4.0 + 0.25,       # map in, two bitmasks in
+    "cleanup_final": 4.0 + 0.25 + 4.0,  # r^2 map in, two bitmasks in, f32 map out (the statistics read it)
+    "stats_order": 8.0,                # f32 map read twice (chunk sums, chunk functions)
     "count_roi": 2.0,
 }
 EDT_FAMILIES = ("edt_x", "edt_y", "edt_z")
@@ -619,7 +620,7 @@ def run_gpu(args, rank, world, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u8/u32/f32 (integer EDT and r^2, f32 map, f64 stats)",
+        "vs_baseline": None, "dtype": "u8/u32/f32 (integer EDT and r^2, f32 map, f64 stats in the reference's order)",
         "data": "synthetic (seeded Gaussian-smoothed noise, thresholded; no public dataset)",
         "config": workload_config(args.workload, sp.bone.shape, world),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n_vox,

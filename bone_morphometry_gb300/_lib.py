@@ -61,6 +61,8 @@ class BmStats(ctypes.Structure):
         ("coefficient_of_variation", ctypes.c_double),
         ("sum", ctypes.c_double),
         ("sum_of_squares", ctypes.c_double),
+        ("exact_sum", ctypes.c_double),
+        ("exact_sum_of_squares", ctypes.c_double),
     ]
 
 

@@ -181,7 +181,9 @@ def local_thickness(volume, phase: Phase = Phase.FOREGROUND, ctx: Context | None
 
 @dataclass
 class DistributionStats:
-    """metrics.rs:27-38, micrometres.  Quantile fields are NaN unless requested."""
+    """metrics.rs:27-38, micrometres.  Quantile fields are NaN unless requested.
+    mean and standard_deviation come from the reference's own sequential sums
+    (metrics.rs:215-241), reproduced bit for bit."""
 
     mean: float
     standard_deviation: float
@@ -194,14 +196,16 @@ class DistributionStats:
     interquartile_range: float
     coefficient_of_variation: float
     count: int = 0
-    sum: float = math.nan
+    sum: float = math.nan              # the reference's sequential f64 accumulators
     sum_of_squares: float = math.nan
+    exact_sum: float = math.nan        # the same sums, exact, rounded once
+    exact_sum_of_squares: float = math.nan
 
     @classmethod
     def from_c(cls, s: BmStats) -> "DistributionStats":
         return cls(s.mean, s.standard_deviation, s.maximum, s.median, s.percentile_10, s.percentile_25,
                    s.percentile_75, s.percentile_90, s.interquartile_range, s.coefficient_of_variation,
-                   int(s.count), s.sum, s.sum_of_squares)
+                   int(s.count), s.sum, s.sum_of_squares, s.exact_sum, s.exact_sum_of_squares)
 
 
 @dataclass

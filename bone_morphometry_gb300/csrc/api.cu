@@ -77,7 +77,7 @@ void release(Buffer& b) {
 const char* const kFamilyName[KF_COUNT] = {"count_roi", "edt_x",     "edt_y",           "edt_z",
                                             "templates", "ridge",     "fill",            "fill_rank",
                                             "fill_bin",  "fill_sites",      "cleanup_final",
-                                            "quantile"};
+                                            "quantile",  "stats_order"};
 
 cudaEvent_t pooled_event(bm_ctx* ctx) {
   if (!ctx->event_pool.empty()) {
@@ -300,13 +300,27 @@ struct PhaseResult {
   unsigned long long sites = 0, selected = 0, ridges = 0;
   uint32_t rmax = 0;
   StatsAccum acc;
+  double osum[2] = {0.0, 0.0};  // the reference's sequential sum and sum of squares
 };
 
-// One phase: EDT (+ local thickness + statistics unless edt_only).
-// d_a / d_b are the device inputs for `mode`; results optionally go to d_edt
-// (u32 EDT), d_map (f32 masked diameters) and d_sq (u32 propagated r^2).
+// The reference's sequential f64 sums of the calibrated map values
+// (metrics.rs:215-224), on stream s, after the statistics accumulator acc has
+// its maximum; results land in ctx->ordout.
+void ordered_sums(bm_ctx* ctx, const float* d_map, long long n, float scale, const StatsAccum* acc, cudaStream_t s) {
+  void* scratch = ensure(ctx, ctx->ordscratch, ordered_sum_scratch_bytes(n), "ordered-sum scratch");
+  double* out = static_cast<double*>(ensure(ctx, ctx->ordout, 2 * sizeof(double), "ordered sums"));
+  timed(ctx, KF_STATS_ORDER, s, "ordered sums", [&] {
+    return launch_ordered_sums(d_map, n, scale, &acc->max_bits, scratch, out, s, &ctx->launches);
+  });
+}
+
+// One phase: EDT (+ local thickness unless edt_only, + the reference-order
+// statistics sums when stats).  d_a / d_b are the device inputs for `mode`;
+// results optionally go to d_edt (u32 EDT), d_map (f32 masked diameters) and
+// d_sq (u32 propagated r^2).
 void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int mode, bool edt_only,
-               uint32_t* d_edt, float* d_map, uint32_t* d_sq, float scale, cudaStream_t s, PhaseResult& res) {
+               uint32_t* d_edt, float* d_map, uint32_t* d_sq, float scale, bool stats, cudaStream_t s,
+               PhaseResult& res) {
   const size_t N = (size_t)dm.n();
   const size_t bits_bytes = (size_t)dm.nw() * dm.h * dm.d * sizeof(uint32_t);
   uint32_t* A = static_cast<uint32_t*>(ensure(ctx, ctx->dist, N * 4, "distance map"));
@@ -369,13 +383,19 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   const int e2s = (int)(tb >> 23);
   const int e_lo = (e2s >= 1 && e2s + kFixedSpan <= 254) ? e2s : 4096;  // 4096: no fixed-point path
   unsigned cgrid = 0;
+  // the statistics' ordered sums read the f32 map: keep one when the caller wants none
+  float* cmap = (stats && !d_map) ? static_cast<float*>(ensure(ctx, ctx->ordmap, N * 4, "thickness map")) : d_map;
   timed(ctx, KF_CLEAN_FINAL, s, "cleanup",
         [&] {
-          return launch_cleanup(F, selbits, dm, static_cast<const float*>(ctx->lutf.ptr), scale, d_map, acc, part,
+          return launch_cleanup(F, selbits, dm, static_cast<const float*>(ctx->lutf.ptr), scale, cmap, acc, part,
                                 e_lo, &cgrid, s, &ctx->launches);
         });
+  if (stats) ordered_sums(ctx, cmap, (long long)N, scale, acc, s);
   std::vector<FixedPartial> hpart(cgrid);
   check(ctx, cudaMemcpyAsync(&res.acc, acc, sizeof(StatsAccum), cudaMemcpyDeviceToHost, s), "stats readback");
+  if (stats)
+    check(ctx, cudaMemcpyAsync(res.osum, ctx->ordout.ptr, 2 * sizeof(double), cudaMemcpyDeviceToHost, s),
+          "stats readback");
   if (cgrid)
     check(ctx, cudaMemcpyAsync(hpart.data(), part, cgrid * sizeof(FixedPartial), cudaMemcpyDeviceToHost, s),
           "stats readback");
@@ -385,14 +405,17 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   res.ridges = hc.ridges;
 }
 
-// nonzero_stats from the exact sums (metrics.rs:228-241; quantile fields NaN).
-int finish_stats(bm_ctx* ctx, const StatsAccum& a, bm_stats* out) {
+// nonzero_stats (metrics.rs:228-241; quantile fields NaN) from the reference's
+// own sequential sums osum = {sum, sum of squares}; the exact sums are
+// reported beside them.
+int finish_stats(bm_ctx* ctx, const StatsAccum& a, const double* osum, bm_stats* out) {
   if (a.count == 0) {
     set_err(ctx, "cannot compute statistics because the selected phase is empty");
     return BM_ERR_EMPTY;
   }
-  double sum, ss;
-  exact_sums_to_double(a, &sum, &ss);
+  double xsum, xss;
+  exact_sums_to_double(a, &xsum, &xss);
+  const double sum = osum[0], ss = osum[1];
   const double c = (double)a.count;
   const double mean = sum / c;
   const double centered = (c * ss - sum * sum) / c;
@@ -409,6 +432,8 @@ int finish_stats(bm_ctx* ctx, const StatsAccum& a, bm_stats* out) {
     out->coefficient_of_variation = sd / mean;
     out->sum = sum;
     out->sum_of_squares = ss;
+    out->exact_sum = xsum;
+    out->exact_sum_of_squares = xss;
   }
   return BM_OK;
 }
@@ -522,7 +547,7 @@ cudaStream_t pick_stream(bm_ctx* ctx, void* stream) {
 int edt_device_impl(bm_ctx* ctx, const uint8_t* d_vol, Dims dm, int phase, uint32_t* d_out, cudaStream_t s) {
   PhaseResult r;
   run_phase(ctx, dm, d_vol, nullptr, phase == BM_PHASE_BACKGROUND ? SEL_BACKGROUND : SEL_FOREGROUND, true, d_out,
-            nullptr, nullptr, 1.0f, s, r);
+            nullptr, nullptr, 1.0f, false, s, r);
   return BM_OK;
 }
 
@@ -530,7 +555,7 @@ int lt_device_impl(bm_ctx* ctx, const uint8_t* d_vol, Dims dm, int phase, float*
                    cudaStream_t s) {
   PhaseResult r;
   run_phase(ctx, dm, d_vol, nullptr, phase == BM_PHASE_BACKGROUND ? SEL_BACKGROUND : SEL_FOREGROUND, false,
-            nullptr, d_out, d_sq, 1.0f, s, r);
+            nullptr, d_out, d_sq, 1.0f, false, s, r);
   return BM_OK;
 }
 
@@ -703,13 +728,13 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
   // 512^3 and below they fill each other's gaps.
   if (!ctx->split_phases || N > kSplitMaxVoxels) {
     float* mb = d_thmap ? d_thmap : qm;
-    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, s, rb);
-    int st = finish_stats(ctx, rb.acc, th);
+    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, true, s, rb);
+    int st = finish_stats(ctx, rb.acc, rb.osum, th);
     if (st) return st;
     if (want_q && th) quantiles(ctx, mb, N, rb.acc.count, spacing, th, s);
     float* mm = d_spmap ? d_spmap : qm;
-    run_phase(ctx, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, s, rm);
-    st = finish_stats(ctx, rm.acc, sp);
+    run_phase(ctx, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, true, s, rm);
+    st = finish_stats(ctx, rm.acc, rm.osum, sp);
     if (st) return st;
     if (want_q && sp) quantiles(ctx, mm, N, rm.acc.count, spacing, sp, s);
     return BM_OK;
@@ -724,7 +749,7 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
     try {
       cudaSetDevice(tw->device);
       check(tw, cudaStreamWaitEvent(tw->stream, ctx->inputs_ready, 0), "stream wait");
-      run_phase(tw, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, tw->stream, rm);
+      run_phase(tw, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, true, tw->stream, rm);
     } catch (const CallError& e) {
       twin_status = e.status;
     } catch (const std::bad_alloc&) {
@@ -734,7 +759,7 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
   });
   int bone_status = BM_OK;
   try {
-    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, s, rb);
+    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, true, s, rb);
   } catch (const CallError& e) {
     bone_status = e.status;
   }
@@ -742,14 +767,14 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
   ctx->launches += tw->launches;
   tw->launches = 0;
   if (bone_status != BM_OK) throw CallError{bone_status};
-  int st = finish_stats(ctx, rb.acc, th);
+  int st = finish_stats(ctx, rb.acc, rb.osum, th);
   if (st) return st;
   if (want_q && th) quantiles(ctx, mb, N, rb.acc.count, spacing, th, s);
   if (twin_status != BM_OK) {
     ctx->last_error = tw->last_error;
     throw CallError{twin_status};
   }
-  st = finish_stats(ctx, rm.acc, sp);
+  st = finish_stats(ctx, rm.acc, rm.osum, sp);
   if (st) return st;
   if (want_q && sp) quantiles(ctx, mm, N, rm.acc.count, spacing, sp, s);
   return BM_OK;
@@ -775,7 +800,7 @@ std::vector<Buffer*> work_buffers(bm_ctx* ctx) {
           &ctx->chainmap,  &ctx->fillmap,    &ctx->selbits,     &ctx->ridgebits, &ctx->ridges, &ctx->accum,
           &ctx->cpart,     &ctx->outmap,     &ctx->outmap2,     &ctx->occ,     &ctx->rank,   &ctx->rvals,
           &ctx->bincounts, &ctx->binoffsets, &ctx->binentries,  &ctx->scanscratch, &ctx->redo, &ctx->qhist,
-          &ctx->qtargets,  &ctx->qmap,       &ctx->rgeo};
+          &ctx->qtargets,  &ctx->qmap,       &ctx->rgeo,        &ctx->ordmap,  &ctx->ordscratch, &ctx->ordout};
 }
 
 size_t cached_bytes(const bm_ctx* ctx) {
@@ -1025,10 +1050,13 @@ int bm_nonzero_stats_device(bm_ctx* ctx, const float* d_values, size_t n, double
     check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
     timed(ctx, KF_QUANTILE, s, "moments kernel",
           [&] { return launch_moments(d_values, (long long)n, (float)scale, acc, s, &ctx->launches); });
+    ordered_sums(ctx, d_values, (long long)n, (float)scale, acc, s);
     StatsAccum ha;
+    double osum[2];
     check(ctx, cudaMemcpyAsync(&ha, acc, sizeof ha, cudaMemcpyDeviceToHost, s), "stats readback");
+    check(ctx, cudaMemcpyAsync(osum, ctx->ordout.ptr, sizeof osum, cudaMemcpyDeviceToHost, s), "stats readback");
     check(ctx, cudaStreamSynchronize(s), "moments kernel");
-    int st = finish_stats(ctx, ha, out);
+    int st = finish_stats(ctx, ha, osum, out);
     if (st) return st;
     if (flags & BM_FLAG_QUANTILES) quantiles(ctx, d_values, (long long)n, ha.count, scale, out, s);
     return BM_OK;
@@ -1046,10 +1074,13 @@ int bm_nonzero_stats(bm_ctx* ctx, const float* values, size_t n, double scale, u
     check(ctx, cudaMemsetAsync(acc, 0, sizeof(StatsAccum), s), "memset");
     timed(ctx, KF_QUANTILE, s, "moments kernel",
           [&] { return launch_moments(d, (long long)n, (float)scale, acc, s, &ctx->launches); });
+    ordered_sums(ctx, d, (long long)n, (float)scale, acc, s);
     StatsAccum ha;
+    double osum[2];
     check(ctx, cudaMemcpyAsync(&ha, acc, sizeof ha, cudaMemcpyDeviceToHost, s), "stats readback");
+    check(ctx, cudaMemcpyAsync(osum, ctx->ordout.ptr, sizeof osum, cudaMemcpyDeviceToHost, s), "stats readback");
     check(ctx, cudaStreamSynchronize(s), "moments kernel");
-    int st = finish_stats(ctx, ha, out);
+    int st = finish_stats(ctx, ha, osum, out);
     if (st) return st;
     if (flags & BM_FLAG_QUANTILES) quantiles(ctx, d, (long long)n, ha.count, scale, out, s);
     return BM_OK;

@@ -166,6 +166,7 @@ enum KernelFamily : int {
   KF_FILL_SITES,
   KF_CLEAN_FINAL,
   KF_QUANTILE,
+  KF_STATS_ORDER,
   KF_COUNT
 };
 
@@ -220,6 +221,7 @@ struct bm_ctx {
   bm::Buffer surf_off, surf_pts;
   bm::Buffer redo;             // per-line flags of the windowed EDT passes
   bm::Buffer qhist, qtargets, qmap;  // quantile histograms, targets, map scratch
+  bm::Buffer ordmap, ordscratch, ordout;  // f32 map for the ordered sums, their scratch, their two results
   uint32_t surf_max = 0;
 
   // profiler: CUDA events around every library launch while enabled

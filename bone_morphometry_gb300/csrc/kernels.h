@@ -114,6 +114,16 @@ cudaError_t launch_sites(const uint2* ridges, const Counters* ctr, unsigned long
                          const uint32_t* selbits, const uint32_t* surf_off, const uint32_t* surf_pts, bool small,
                          Dims dm, uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
 
+// The sum and the sum of squares of x = f32(raw * scale) as f64 over the finite
+// positive raw values of map[0 .. n), each accumulated in index order with one
+// f64 rounding per value -- the reference's own sequence (metrics.rs:215-224),
+// reproduced exactly (ordered.cu).  out[0] = sum, out[1] = sum of squares.
+// maxbits: device pointer to the f32 bits of the largest such value (the
+// statistics accumulator's max_bits), which scales the approximate sums.
+size_t ordered_sum_scratch_bytes(long long n);
+cudaError_t launch_ordered_sums(const float* map, long long n, float scale, const uint32_t* maxbits, void* scratch,
+                                double* out, cudaStream_t s, unsigned long long* launches);
+
 // Exact moment sums of f32(raw * scale) over the finite positive raw values.
 cudaError_t launch_moments(const float* map, long long n, float scale, StatsAccum* acc, cudaStream_t s,
                            unsigned long long* launches);

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BM_ABI_VERSION 1
+#define BM_ABI_VERSION 2
 
 typedef enum bm_status {
   BM_OK = 0,
@@ -56,8 +56,12 @@ typedef enum bm_phase { BM_PHASE_FOREGROUND = 0, BM_PHASE_BACKGROUND = 1 } bm_ph
 /* metrics.rs:27-38 (DistributionStats), in micrometres.  Quantile fields are
  * NaN unless BM_FLAG_QUANTILES was given (metrics.rs:242-255); then
  * interquartile_range = p75 - p25 and coefficient_of_variation = sd / mean.
- * sum and sum_of_squares are the exact sums of the scaled f32 values rounded
- * once to f64 (the reference accumulates them sequentially). */
+ * sum and sum_of_squares are the reference's own f64 accumulators
+ * (metrics.rs:215-224: the scaled f32 values added one after the other in
+ * index order, one rounding per value), reproduced bit for bit; mean and
+ * standard_deviation follow from them with the reference's formulas
+ * (metrics.rs:232-241).  exact_sum and exact_sum_of_squares are the same sums
+ * computed exactly and rounded once to f64 (no counterpart in the reference). */
 typedef struct bm_stats {
   uint64_t count;
   double mean;
@@ -72,6 +76,8 @@ typedef struct bm_stats {
   double coefficient_of_variation;
   double sum;
   double sum_of_squares;
+  double exact_sum;
+  double exact_sum_of_squares;
 } bm_stats;
 
 /* Flags for bm_tbth_tbsp*. */

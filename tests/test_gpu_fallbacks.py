@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from refstats import assert_reference_stats
 from bone_morphometry_gb300 import (BoneMorphometryError, Phase, _lib, analyze_thickness,
                                     euclidean_distance_transform_squared, local_thickness)
 
@@ -58,8 +59,7 @@ def test_scatter_fill_fallback_tbth_tbsp(gpu_ctx):
     for sel, got, gmap in ((True, res.thickness, res.thickness_map), (False, res.spacing, res.spacing_map)):
         ref = O.local_thickness(O.phase_inside(bone, roi, sel), O.FOREGROUND)
         assert np.array_equal(gmap.view(np.uint32), ref.thickness.view(np.uint32))
-        n, s, ss, mx = O.exact_moment_sums(ref.thickness, 12.5)
-        assert (got.count, got.sum, got.sum_of_squares, got.maximum) == (n, s, ss, mx)
+        assert_reference_stats(got, ref.thickness, 12.5)
 
 
 def test_tma_wait_timeout_reports_and_recovers(gpu_ctx):

@@ -1,5 +1,5 @@
-"""GPU parity through the C ABI against the CPU oracle (bit-exact maps, stats
-within the stated tolerance).  Marked gpu."""
+"""GPU parity through the C ABI against the CPU oracle: bit-exact maps and
+statistics identical to the reference's (its own sequential f64 sums).  Marked gpu."""
 
 import numpy as np
 import pytest
@@ -10,15 +10,9 @@ from bone_morphometry_gb300 import (BinaryVolume, BoneMorphometryError, Phase, a
 from bone_morphometry_gb300 import _lib
 from bone_morphometry_gb300 import synthetic as S
 
-pytestmark = pytest.mark.gpu
+from refstats import assert_reference_stats
 
-# Relative tolerance of the Tb.Th / Tb.Sp mean, SD and max against the
-# reference's own sequential f64 accumulation.  The GPU sums exactly (bitwise
-# equal to oracle.exact_moment_sums + the reference formulas); the sequential
-# sum of n positive terms differs from the exact one by at most ~n*eps, and the
-# SD formula amplifies that by ~ mean^2 / var.
-def seq_tol(n, amplification=1.0):
-    return max(1e-12, 4.0 * n * 2.0 ** -53 * amplification)
+pytestmark = pytest.mark.gpu
 
 
 def rand_volume(shape, p, seed):
@@ -163,16 +157,7 @@ def test_background_matches_complement(gpu_ctx):
 
 
 def check_stats(got, ref_map, scale):
-    n, s, ss, mx = O.exact_moment_sums(ref_map, scale)
-    mean, sd, mxr = O.stats_from_sums(n, s, ss, mx)
-    assert got.count == n
-    assert got.sum == s and got.sum_of_squares == ss
-    assert got.mean == mean and got.standard_deviation == sd and got.maximum == mxr
-    seq = O.nonzero_stats(ref_map, scale)
-    amp = (seq.mean / seq.sd) ** 2 if seq.sd > 0 else 1.0
-    assert abs(got.mean - seq.mean) <= seq_tol(n) * abs(seq.mean)
-    assert abs(got.maximum - seq.max) == 0.0
-    assert abs(got.standard_deviation - seq.sd) <= seq_tol(n, amp) * abs(seq.sd) + 1e-300
+    assert_reference_stats(got, ref_map, scale)
 
 
 def test_tbth_tbsp_plain_128(gpu_ctx, site_method):

@@ -8,6 +8,7 @@ import pytest
 import oracle as O
 from bone_morphometry_gb300 import BoneMorphometryError, FeatureMode, analyze_thickness, nonzero_stats
 from bone_morphometry_gb300 import synthetic as S
+from refstats import assert_reference_stats
 
 pytestmark = pytest.mark.gpu
 
@@ -60,9 +61,7 @@ def test_random_values_exact(gpu_ctx, n, seed):
     if not (v > 0).any():
         v[0] = 1.5
     st = nonzero_stats(v, 19.5, True, ctx=gpu_ctx)
-    cnt, s, ss, mx = O.exact_moment_sums(v, 19.5)
-    mean, sd, mxr = O.stats_from_sums(cnt, s, ss, mx)
-    assert (st.count, st.mean, st.standard_deviation, st.maximum) == (cnt, mean, sd, mxr)
+    assert_reference_stats(st, v, 19.5)
     check_quantiles(st, v, 19.5)
 
 
@@ -114,14 +113,65 @@ def test_volume_metrics_random(gpu_ctx):
 
 @pytest.mark.parametrize("spacing", [1e-39, 3e-38, 0.37, 7.5e33])
 def test_tbth_tbsp_exact_sums_at_extreme_spacings(gpu_ctx, spacing):
-    """Fixed-point and per-exponent statistic paths (subnormal, tiny, ordinary
-    and huge calibrations) against an exact summation of the oracle's maps."""
+    """Fixed-point and per-exponent exact-sum paths and the reference-order sums
+    (subnormal, tiny, ordinary and huge calibrations) against the oracle."""
     sp = S.make_specimen((24, 26, 28), 2.0, 0.3, "cylinder", 11.0, spacing, 41)
     res = analyze_thickness(sp.bone, sp.roi, spacing, ctx=gpu_ctx)
     for sel, got in ((True, res.thickness), (False, res.spacing)):
         ref = O.local_thickness(O.phase_inside(sp.bone, sp.roi, sel), O.FOREGROUND).thickness
-        n, s, ss, mx = O.exact_moment_sums(ref, spacing)
-        mean, sd, mxr = O.stats_from_sums(n, s, ss, mx)
-        assert got.count == n
-        assert got.sum == s and got.sum_of_squares == ss
-        assert got.mean == mean and got.standard_deviation == sd and got.maximum == mxr
+        assert_reference_stats(got, ref, spacing)
+
+
+# -- the reference-order sums on maps made to stress them --------------------------------------
+
+def _ties_map(n, seed):
+    """A huge first value, then odd multiples of half the running sum's ulp
+    (round-half-even decided by the sum's parity), values below half an ulp
+    (lost), skipped entries and ordinary values."""
+    rng = np.random.default_rng(seed)
+    v = np.zeros(n, np.float32)
+    kind = rng.random(n)
+    odd = (2 * rng.integers(1, 1 << 15, size=n) + 1).astype(np.float64) * 128.0
+    v[kind < 0.5] = odd[kind < 0.5].astype(np.float32)
+    small = (kind >= 0.5) & (kind < 0.7)
+    v[small] = rng.integers(1, 128, size=int(small.sum())).astype(np.float32)
+    other = kind >= 0.8
+    v[other] = (rng.random(int(other.sum())) * 1e6).astype(np.float32)
+    v[0] = 2.0 ** 60
+    return v
+
+
+@pytest.mark.parametrize("n,seed", [(1, 0), (2, 1), (255, 2), (256, 3), (257, 4), (8191, 5), (8193, 6),
+                                    (300_001, 7), (2_100_000, 8)])
+def test_reference_order_sums_on_ties(gpu_ctx, n, seed):
+    v = _ties_map(n, seed)
+    for scale in (1.0, 0.75):
+        assert_reference_stats(nonzero_stats(v, scale, ctx=gpu_ctx), v, scale)
+
+
+@pytest.mark.parametrize("n,seed", [(5_000_000, 11), (33_554_433, 12)])
+def test_reference_order_sums_many_crossings(gpu_ctx, n, seed):
+    """Values over eight decades after tiny ones: the running sums cross more
+    than a hundred binades, some within one chunk of 256 entries."""
+    rng = np.random.default_rng(seed)
+    v = (10.0 ** rng.uniform(-3, 5, size=n)).astype(np.float32)
+    v[rng.random(n) < 0.4] = 0.0
+    v[: 1000] = (10.0 ** rng.uniform(-30, -20, size=1000)).astype(np.float32)
+    assert_reference_stats(nonzero_stats(v, 19.5, ctx=gpu_ctx), v, 19.5)
+
+
+def test_reference_order_sums_leading_zeros(gpu_ctx):
+    """Millions of empty entries before the first value (outside the ROI)."""
+    v = np.zeros(12_000_000, np.float32)
+    rng = np.random.default_rng(13)
+    v[9_000_000:] = (rng.random(3_000_000) * 300).astype(np.float32)
+    assert_reference_stats(nonzero_stats(v, 8.0, ctx=gpu_ctx), v, 8.0)
+
+
+def test_reference_order_sums_overflow_to_inf(gpu_ctx):
+    """raw * scale overflowing f32 gives +inf values: sums +inf as in the reference."""
+    v = np.array([0, 3.0, 2.0e30, 5.0, 0, 1e-3] * 1000, np.float32)
+    st = nonzero_stats(v, 1e10, ctx=gpu_ctx)
+    seq = O.nonzero_stats(v, 1e10)
+    assert st.sum == seq.sum == float("inf") and st.count == seq.count
+    assert st.sum_of_squares == seq.sum_sq and st.mean == seq.mean and st.maximum == seq.max
