@@ -243,8 +243,9 @@ uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, u
   } else {
     ensure_surf(ctx, rmax);
   }
+  uint32_t* order = static_cast<uint32_t*>(ensure(ctx, ctx->tileorder, tile_order_words(dm) * 4, "tile order"));
   timed(ctx, KF_FILL, s, "tile fill kernel", [&] {
-    return launch_tile_fill(entries, offsets, rvals, rgeo, info, selbits, dm, F, s, &ctx->launches);
+    return launch_tile_fill(entries, offsets, rvals, rgeo, info, selbits, dm, order, F, s, &ctx->launches);
   });
   if (chains) {
     timed(ctx, KF_FILL_SITES, s, "chain y pass",
@@ -388,7 +389,7 @@ void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int
   timed(ctx, KF_CLEAN_FINAL, s, "cleanup",
         [&] {
           return launch_cleanup(F, selbits, dm, static_cast<const float*>(ctx->lutf.ptr), scale, cmap, acc, part,
-                                e_lo, &cgrid, s, &ctx->launches);
+                                e_lo, &ctr->tile_next[1], &cgrid, s, &ctx->launches);
         });
   if (stats) ordered_sums(ctx, cmap, (long long)N, scale, acc, s);
   std::vector<FixedPartial> hpart(cgrid);
@@ -800,7 +801,8 @@ std::vector<Buffer*> work_buffers(bm_ctx* ctx) {
           &ctx->chainmap,  &ctx->fillmap,    &ctx->selbits,     &ctx->ridgebits, &ctx->ridges, &ctx->accum,
           &ctx->cpart,     &ctx->outmap,     &ctx->outmap2,     &ctx->occ,     &ctx->rank,   &ctx->rvals,
           &ctx->bincounts, &ctx->binoffsets, &ctx->binentries,  &ctx->scanscratch, &ctx->redo, &ctx->qhist,
-          &ctx->qtargets,  &ctx->qmap,       &ctx->rgeo,        &ctx->ordmap,  &ctx->ordscratch, &ctx->ordout};
+          &ctx->qtargets,  &ctx->qmap,       &ctx->rgeo,        &ctx->ordmap,  &ctx->ordscratch, &ctx->ordout,
+          &ctx->tileorder};
 }
 
 size_t cached_bytes(const bm_ctx* ctx) {

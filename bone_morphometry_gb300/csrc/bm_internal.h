@@ -150,6 +150,7 @@ struct Counters {  // device-side counters of one phase
   unsigned long long ridges;
   unsigned int rmax;
   unsigned int status;          // nonzero: a bounded wait gave up / capacity exceeded
+  unsigned int tile_next[2];    // next tile to take: ridge pass, cleanup pass (dynamic tile scheduling)
 };
 
 // Kernel families timed by the context's profiler (bm_profile_*).
@@ -222,6 +223,7 @@ struct bm_ctx {
   bm::Buffer redo;             // per-line flags of the windowed EDT passes
   bm::Buffer qhist, qtargets, qmap;  // quantile histograms, targets, map scratch
   bm::Buffer ordmap, ordscratch, ordout;  // f32 map for the ordered sums, their scratch, their two results
+  bm::Buffer tileorder;        // the fill's tile order (heaviest first) and its bucket counts
   uint32_t surf_max = 0;
 
   // profiler: CUDA events around every library launch while enabled

@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(kFillThreads, 4)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
                  const uint32_t* __restrict__ rvals, const uint4* __restrict__ rgeo, const FillInfo* __restrict__ info,
                  const uint32_t* __restrict__ selbits, Dims dm, VoxelDecoder vd, Geom g,
-                 uint32_t* __restrict__ fillmap) {
+                 const uint32_t* __restrict__ order, uint32_t* __restrict__ fillmap) {
   extern __shared__ uint32_t smem[];
   uint16_t* val = reinterpret_cast<uint16_t*>(smem);       // kRows * 32 half-words
   uint32_t* usel = smem + kRows * 16;                        // kRows
@@ -282,7 +282,8 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
   const int hl = lane & 15, half = lane >> 4;
   const unsigned lanes_below = (1u << lane) - 1u;
   uint32_t parity = 0;  // which item counter the next round uses
-  for (long long tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x) {
+  for (long long k = blockIdx.x; k < g.ntiles; k += gridDim.x) {
+    const long long tile = order[k];  // heaviest tiles first
     const int tx = (int)(tile % g.ntx);
     const int ty = (int)((tile / g.ntx) % g.nty);
     const int tz = (int)(tile / ((long long)g.ntx * g.nty));
@@ -660,17 +661,78 @@ cudaError_t launch_surf(bool count, uint32_t lo, uint32_t hi, uint32_t* surf_cnt
   return cudaGetLastError();
 }
 
+namespace {
+
+// Tile order of the fill: heaviest first (largest-processing-time order), so
+// that the last CTAs to start are short ones and the launch has no long
+// tail.  A tile's weight is its ball-entry count; tiles are counting-sorted
+// into buckets of a quarter octave of that count, descending.
+constexpr int kOrderBuckets = 132;
+
+__device__ __forceinline__ int weight_bucket(uint32_t c) {
+  if (c == 0u) return 0;
+  const int b = 1 + (int)(4.0f * __log2f((float)c));
+  return b < kOrderBuckets - 1 ? b : kOrderBuckets - 1;
+}
+
+__device__ __forceinline__ uint32_t tile_entries(const uint32_t* offsets, uint32_t nR, long long t) {
+  return offsets[(t + 1) * (long long)nR] - offsets[t * (long long)nR];
+}
+
+__global__ void tile_weight_hist_kernel(const uint32_t* __restrict__ offsets, const FillInfo* __restrict__ info,
+                                        long long ntiles, uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[kOrderBuckets];
+  for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  const uint32_t nR = info->nR;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += (long long)gridDim.x * blockDim.x)
+    atomicAdd(&h[weight_bucket(tile_entries(offsets, nR, t))], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// hist -> start of every bucket in descending bucket order (one thread).
+__global__ void tile_weight_scan_kernel(uint32_t* __restrict__ hist) {
+  uint32_t run = 0;
+  for (int b = kOrderBuckets - 1; b >= 0; --b) {
+    const uint32_t c = hist[b];
+    hist[b] = run;
+    run += c;
+  }
+}
+
+__global__ void tile_weight_scatter_kernel(const uint32_t* __restrict__ offsets, const FillInfo* __restrict__ info,
+                                           long long ntiles, uint32_t* __restrict__ start,
+                                           uint32_t* __restrict__ order) {
+  const uint32_t nR = info->nR;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += (long long)gridDim.x * blockDim.x)
+    order[atomicAdd(&start[weight_bucket(tile_entries(offsets, nR, t))], 1u)] = (uint32_t)t;
+}
+
+}  // namespace
+
+size_t tile_order_words(Dims dm) { return (size_t)geom_of(dm).ntiles + kOrderBuckets; }
+
 cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
                              const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm,
-                             uint32_t* fillmap, cudaStream_t s, unsigned long long* launches) {
+                             uint32_t* order_scratch, uint32_t* fillmap, cudaStream_t s, unsigned long long* launches) {
   const Geom g = geom_of(dm);
   const size_t smem = kTileFillSmemWords * sizeof(uint32_t);
   cudaError_t e = cudaFuncSetAttribute(tile_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  uint32_t* hist = order_scratch;
+  uint32_t* order = order_scratch + kOrderBuckets;
+  e = cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  const unsigned ob = blocks_for(g.ntiles, 256, 152 * 4);
+  tile_weight_hist_kernel<<<ob, 256, 0, s>>>(offsets, info, g.ntiles, hist);
+  tile_weight_scan_kernel<<<1, 1, 0, s>>>(hist);
+  tile_weight_scatter_kernel<<<ob, 256, 0, s>>>(offsets, info, g.ntiles, hist, order);
   const long long grid = g.ntiles < (1LL << 31) - 1 ? g.ntiles : (1LL << 31) - 1;
   tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, rgeo, info, selbits, dm,
-                                                               VoxelDecoder::of(dm), g, fillmap);
-  ++*launches;
+                                                               VoxelDecoder::of(dm), g, order, fillmap);
+  *launches += 4;
   return cudaGetLastError();
 }
 

@@ -81,9 +81,10 @@ cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long 
 // fixed point, one FixedPartial per CTA in part[0 .. *grid); the others go to
 // acc's per-exponent sums.  At most kCleanupMaxGrid CTAs.
 constexpr unsigned kCleanupMaxGrid = 4096;
+// tile_next: a zeroed counter the CTAs take tiles from.
 cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const float* dia, float scale,
-                           float* outmap, StatsAccum* acc, FixedPartial* part, int e_lo, unsigned* grid,
-                           cudaStream_t s, unsigned long long* launches);
+                           float* outmap, StatsAccum* acc, FixedPartial* part, int e_lo, unsigned* tile_next,
+                           unsigned* grid, cudaStream_t s, unsigned long long* launches);
 cudaError_t launch_dia_table(const uint4* lut, uint32_t n, float* dia, cudaStream_t s, unsigned long long* launches);
 
 // Tile-owned fill (fill.cu).
@@ -104,9 +105,11 @@ cudaError_t launch_surf(bool count, uint32_t lo, uint32_t hi, uint32_t* surf_cnt
                         uint32_t* surf_pts, cudaStream_t s, unsigned long long* launches);
 // Selected voxels of every tile from the binned balls; non-selected voxels get 0.
 // selbits: the phase's row-padded selection bitmask (edt_x output).
+// order_scratch: tile_order_words(dm) words (the tiles' processing order).
+size_t tile_order_words(Dims dm);
 cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
                              const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm,
-                             uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
+                             uint32_t* order_scratch, uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
 // Non-selected voxels on each ridge's sphere: atomic max of r2 (after the tile
 // fill).  surf_off / surf_pts: the lattice-point table covering every ridge r2;
 // small: 8 lanes per ridge instead of 16 (spheres of about 40 points or fewer).

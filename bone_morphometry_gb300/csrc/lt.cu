@@ -168,8 +168,9 @@ __global__ void __launch_bounds__(kCleanThreads, 3)
 cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict__ selbits, Dims dm,
                     const float* __restrict__ dia, float scale, float* __restrict__ outmap,
                     StatsAccum* __restrict__ acc, FixedPartial* __restrict__ part, int e_lo, int ntx, int nty,
-                    int ntz) {
+                    int ntz, unsigned* __restrict__ tile_next) {
   __shared__ uint32_t T[kCSZ * kCSY * kCSX];         // f32 diameter bits of the r^2 map
+  __shared__ uint32_t s_tile;
   __shared__ unsigned long long nz[kCSZ * kCSY];     // bit x: T != 0 (or out of volume)
   __shared__ unsigned long long inr[kCSZ * kCSY];    // bit x: interior (pass-1 value kept)
   __shared__ unsigned long long own[kCSZ * kCSY];    // bit x: T != 0 inside the volume
@@ -196,7 +197,13 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
   unsigned long long fx1 = 0;
   unsigned __int128 fx2 = 0;
   const long long ntiles = (long long)ntx * nty * ntz;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  // tiles are taken from a counter as CTAs free up (their costs vary widely)
+  for (;;) {
+    __syncthreads();  // every thread has read s_tile
+    if (tid == 0) s_tile = atomicAdd(tile_next, 1u);
+    __syncthreads();
+    const long long tile = s_tile;
+    if (tile >= ntiles) break;
     const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
     const int x0 = tx * kCTX, y0 = ty * kCTY, z0 = tz * kCTZ;
     // a tile without selected voxels (outside the ROI, say) has a zero output and
@@ -381,10 +388,17 @@ ridge_tile_kernel(const uint32_t* __restrict__ dist, const uint32_t* __restrict_
   __shared__ uint32_t D[kRSZ * kRSY * kRSX];
   __shared__ uint32_t s_wcnt[8];
   __shared__ unsigned long long s_base;
+  __shared__ uint32_t s_tile;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long ntiles = (long long)ntx * nty * ntz;
   const int nw = dm.nw();
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  // tiles are taken from a counter as CTAs free up (their costs vary widely)
+  for (;;) {
+    __syncthreads();  // every thread has read s_tile
+    if (tid == 0) s_tile = atomicAdd(&ctr->tile_next[0], 1u);
+    __syncthreads();
+    const long long tile = s_tile;
+    if (tile >= ntiles) break;
     const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
     const int x0 = tx * kRTX, y0 = ty * kRTY, z0 = tz * kRTZ;
     // ridges are selected voxels: a tile without any has none
@@ -532,15 +546,15 @@ cudaError_t launch_fill(const uint2* ridges, const Counters* ctr, unsigned long 
 }
 
 cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dims dm, const float* dia, float scale,
-                           float* outmap, StatsAccum* acc, FixedPartial* part, int e_lo, unsigned* grid,
-                           cudaStream_t s, unsigned long long* launches) {
+                           float* outmap, StatsAccum* acc, FixedPartial* part, int e_lo, unsigned* tile_next,
+                           unsigned* grid, cudaStream_t s, unsigned long long* launches) {
   const int ntx = (dm.w + kCTX - 1) / kCTX, nty = (dm.h + kCTY - 1) / kCTY, ntz = (dm.d + kCTZ - 1) / kCTZ;
   const long long tiles = (long long)ntx * nty * ntz;
   unsigned g = resident_grid(cleanup_tile_kernel, kCleanThreads, 0, tiles);
   if (g > kCleanupMaxGrid) g = kCleanupMaxGrid;
   *grid = g;
   cleanup_tile_kernel<<<g, kCleanThreads, 0, s>>>(fillmap, selbits, dm, dia, scale, outmap, acc, part, e_lo, ntx, nty,
-                                                  ntz);
+                                                  ntz, tile_next);
   ++*launches;
   return cudaGetLastError();
 }
