@@ -22,7 +22,7 @@
 //
 // The pipeline.  The map is cut into chunks of kChunk voxels in index order.
 //   1. approximate sums of v and v*v per chunk (f32, on values scaled by a
-//      power of two) and per block of 32 chunks (f64);
+//      power of two) and per block of 32 chunks (fixed point);
 //   2. an exclusive scan of the block sums: approximate prefix sums;
 //   3. per chunk, the binade the running sum is predicted to stay in (from the
 //      approximate prefix, with a relative margin), and the chunk's function
@@ -54,10 +54,15 @@ constexpr int kChunk = 256;                      // voxels per chunk
 constexpr unsigned long long kTwo53 = 1ull << 53;
 constexpr unsigned long long kSat = 1ull << 54;  // saturated increment: never valid
 // Relative margin of the binade prediction.  The approximate prefix sums come
-// from f32 chunk sums (relative error ~2^-21 each, shrinking relative to the
-// prefix as it grows); the sequential sum differs from the exact prefix by
-// ~sqrt(k) 2^-53.  A miss only sends a chunk to the replay.
-constexpr double kMargin = 1.0 / 1048576.0;  // 2^-20
+// from f32 chunk sums in fixed point (errors of ~2^-21 of a chunk each,
+// shrinking relative to the prefix as it grows); the sequential sum differs
+// from the exact prefix by ~sqrt(k) 2^-53.  A miss only sends a chunk to the
+// replay.
+constexpr double kMargin = 1.0 / 16777216.0;  // 2^-24
+// Fixed-point scale of the approximate sums (values scaled into [1, 2)):
+// 2^24 units per unit, so a 2^32-voxel map's sums of squares fit 64 bits.
+constexpr float kFix = 16777216.0f;
+constexpr double kUnfix = 1.0 / 16777216.0;
 
 // meta word of a function: 0 = invalid (no prediction); bit 2 = identity valid
 // in every binade; else bits 3.. hold E + 2048; bits 0, 1 = out parity for
@@ -214,12 +219,16 @@ __device__ __forceinline__ float norm_factor(uint32_t maxbits) {
   return __uint_as_float((uint32_t)(254 - max_exponent_field(maxbits)) << 23);  // 2^(127 - ef)
 }
 
+__device__ __forceinline__ unsigned long long to_fixed(float x) {
+  return (unsigned long long)__fmul_rn(x, kFix);
+}
+
 // 1. Approximate sums per chunk of v and v^2 (scaled by norm_factor, in f32)
-// and per block of 32 chunks (f64); one warp per block, lane j keeps chunk j.
+// and per block of 32 chunks (fixed point); one warp per block, lane j keeps chunk j.
 __global__ void __launch_bounds__(256)
 osum_chunk_kernel(const float* __restrict__ map, long long n, float scale, long long nchunks,
                   const uint32_t* __restrict__ maxbits, float* __restrict__ cs, float* __restrict__ cq,
-                  double* __restrict__ bs, double* __restrict__ bq) {
+                  unsigned long long* __restrict__ bs, unsigned long long* __restrict__ bq) {
   const int lane = threadIdx.x & 31;
   const long long blk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long c0 = blk * 32;
@@ -251,7 +260,8 @@ osum_chunk_kernel(const float* __restrict__ map, long long n, float scale, long 
     cs[c0 + lane] = my_s;
     cq[c0 + lane] = my_q;
   }
-  double ts = my_s, tq = my_q;
+  unsigned long long ts = c0 + lane < nchunks ? to_fixed(my_s) : 0ull;
+  unsigned long long tq = c0 + lane < nchunks ? to_fixed(my_q) : 0ull;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     ts += __shfl_xor_sync(0xffffffffu, ts, o);
@@ -263,21 +273,22 @@ osum_chunk_kernel(const float* __restrict__ map, long long n, float scale, long 
   }
 }
 
-// 2. Exclusive scan of the block sums in place (one CTA of 1024 threads).
-__global__ void __launch_bounds__(1024) osum_scan_kernel(double* __restrict__ bs, double* __restrict__ bq, long long nb) {
-  __shared__ double ws[32], wq[32];
+// 2. Exclusive scan of the block sums in place, fixed point (one CTA of 1024 threads).
+__global__ void __launch_bounds__(1024) osum_scan_kernel(unsigned long long* __restrict__ bs,
+                                                         unsigned long long* __restrict__ bq, long long nb) {
+  __shared__ unsigned long long ws[32], wq[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long per = (nb + 1023) / 1024;
   const long long b0 = (long long)tid * per, b1 = b0 + per < nb ? b0 + per : nb;
-  double ls = 0.0, lq = 0.0;
+  unsigned long long ls = 0, lq = 0;
   for (long long b = b0; b < b1; ++b) {
     ls += bs[b];
     lq += bq[b];
   }
-  double is = ls, iq = lq;  // inclusive scan of the threads' totals
+  unsigned long long is = ls, iq = lq;  // inclusive scan of the threads' totals
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const double us = __shfl_up_sync(0xffffffffu, is, o), uq = __shfl_up_sync(0xffffffffu, iq, o);
+    const unsigned long long us = __shfl_up_sync(0xffffffffu, is, o), uq = __shfl_up_sync(0xffffffffu, iq, o);
     if (lane >= o) {
       is += us;
       iq += uq;
@@ -289,10 +300,10 @@ __global__ void __launch_bounds__(1024) osum_scan_kernel(double* __restrict__ bs
   }
   __syncthreads();
   if (warp == 0) {
-    double a = ws[lane], b = wq[lane];
+    unsigned long long a = ws[lane], b = wq[lane];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const double ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
+      const unsigned long long ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
       if (lane >= o) {
         a += ua;
         b += ub;
@@ -302,9 +313,9 @@ __global__ void __launch_bounds__(1024) osum_scan_kernel(double* __restrict__ bs
     wq[lane] = b - wq[lane];
   }
   __syncthreads();
-  double rs = ws[warp] + is - ls, rq = wq[warp] + iq - lq;
+  unsigned long long rs = ws[warp] + is - ls, rq = wq[warp] + iq - lq;
   for (long long b = b0; b < b1; ++b) {
-    const double ts = bs[b], tq = bq[b];
+    const unsigned long long ts = bs[b], tq = bq[b];
     bs[b] = rs;
     bq[b] = rq;
     rs += ts;
@@ -389,8 +400,8 @@ constexpr int kTileStride = 33;  // words per row of a warp's transpose tile (co
 __global__ void __launch_bounds__(256)
 osum_fn_kernel(const float* __restrict__ map, long long n, float scale, long long nchunks,
                const uint32_t* __restrict__ maxbits, const float* __restrict__ cs, const float* __restrict__ cq,
-               const double* __restrict__ bps, const double* __restrict__ bpq, Level s0, Level q0, Level s1,
-               Level q1) {
+               const unsigned long long* __restrict__ bps, const unsigned long long* __restrict__ bpq, Level s0,
+               Level q0, Level s1, Level q1) {
   __shared__ float tile[8][32 * kTileStride];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long blk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -398,11 +409,11 @@ osum_fn_kernel(const float* __restrict__ map, long long n, float scale, long lon
   if (c0 >= nchunks) return;
   float* T = tile[warp];
   const bool mine = c0 + lane < nchunks;
-  const double as = mine ? (double)cs[c0 + lane] : 0.0, aq = mine ? (double)cq[c0 + lane] : 0.0;
-  double ps = as, pq = aq;  // inclusive scan within the block
+  const unsigned long long as = mine ? to_fixed(cs[c0 + lane]) : 0ull, aq = mine ? to_fixed(cq[c0 + lane]) : 0ull;
+  unsigned long long ps = as, pq = aq;  // inclusive scan within the block
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const double us = __shfl_up_sync(0xffffffffu, ps, o), uq = __shfl_up_sync(0xffffffffu, pq, o);
+    const unsigned long long us = __shfl_up_sync(0xffffffffu, ps, o), uq = __shfl_up_sync(0xffffffffu, pq, o);
     if (lane >= o) {
       ps += us;
       pq += uq;
@@ -410,7 +421,8 @@ osum_fn_kernel(const float* __restrict__ map, long long n, float scale, long lon
   }
   // the approximate sums are of values scaled by 2^(127 - ef): undo it in the binade
   const int shift = max_exponent_field(*maxbits) - 127;
-  const int es = predict(bps[blk] + ps - as, as, shift), eq = predict(bpq[blk] + pq - aq, aq, 2 * shift);
+  const int es = predict((double)(bps[blk] + ps - as) * kUnfix, (double)as * kUnfix, shift);
+  const int eq = predict((double)(bpq[blk] + pq - aq) * kUnfix, (double)aq * kUnfix, 2 * shift);
   const int ems = es == INT_MIN ? 0 : es - 52, emq = eq == INT_MIN ? 0 : eq - 52;
   Acc A{0ull, 0ull, 0u, 1u}, Q{0ull, 0ull, 0u, 1u};
   bool any = false;
@@ -486,55 +498,75 @@ struct Walk {
   int nlev;
 };
 
-// Replays chunk c from state s as the reference adds, value after value: lane
-// 0 keeps s as an integer count of its binade's ulps and adds each value's
-// rounded increment (round half to even on that count), and falls back to a
-// hardware f64 addition -- the reference's own operation -- for the first
-// value (s = 0), for a value that leaves the binade, and for +inf.  The
-// chunk is staged through shared memory by the warp; s is broadcast back.
+// Replays chunk c from state s as the reference adds, value after value.  s
+// is kept as an integer count u of its binade's ulps; every value's rounded
+// increment a (and whether it is a tie) for the binade s starts the chunk in
+// is computed by the warp in parallel, then lane 0 adds them in order (round
+// half to even on u for a tie) and falls back to a hardware f64 addition --
+// the reference's own operation -- for the first value (s = 0), for a value
+// that leaves the binade, and for +inf; after such a change of binade it
+// computes the remaining increments itself.  s is broadcast back.
+struct ReplayBuf {
+  unsigned long long a[kChunk];
+  float raw[kChunk];
+  uint8_t flag[kChunk];  // 0: skipped; bit 0: value; bit 1: a fits the binade; bit 2: tie
+};
+
+__device__ __forceinline__ uint8_t increment(const Term& t, int E, unsigned long long& a) {
+  if (!t.M) return 0;
+  if (t.k == INT_MAX) {
+    a = 0;
+    return 1;  // +inf: f64 path
+  }
+  const int sh = (E - 52) - t.k;
+  a = 0;
+  if (sh <= 0) {
+    const bool fits = sh > -54 && (t.M >> (54 + sh)) == 0;
+    a = fits ? t.M << -sh : 0;
+    return fits ? 3 : 1;
+  }
+  if (sh < 64) {
+    const unsigned long long rem = t.M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    a = (t.M >> sh) + (rem > half ? 1ull : 0ull);
+    return rem == half ? 7 : 3;
+  }
+  return 3;  // far below half an ulp: a = 0
+}
+
 __device__ void replay_chunk(const float* __restrict__ map, long long n, float scale, bool sq, long long c, double& s,
-                             int lane, float* buf) {
+                             int lane, ReplayBuf& rb) {
+  const bool start_units = isfinite(s) && s > 0.0;
+  const int E0 = start_units ? binade_of(s) : 0;
   for (int j = lane; j < kChunk; j += 32) {
     const long long idx = c * kChunk + j;
-    buf[j] = idx < n ? map[idx] : 0.0f;
+    const float raw = idx < n ? map[idx] : 0.0f;
+    const Term t = term(raw, scale, sq);
+    unsigned long long a = 0;
+    rb.raw[j] = raw;
+    rb.flag[j] = start_units ? increment(t, E0, a) : (t.M ? 1 : 0);
+    rb.a[j] = a;
   }
   __syncwarp();
   if (lane == 0) {
     double acc = s;
-    int E = 0;
-    unsigned long long u = 0;
-    bool in_units = isfinite(acc) && acc > 0.0;  // u / E hold acc
-    if (in_units) {
-      E = binade_of(acc);
-      u = units_of(acc);
-    }
+    bool in_units = start_units;  // u / E hold acc
+    int E = E0;
+    unsigned long long u = start_units ? units_of(acc) : 0ull;
     for (int j = 0; j < kChunk; ++j) {
-      const float raw = buf[j];
-      const Term t = term(raw, scale, sq);
-      if (!t.M) continue;  // skipped (metrics.rs:216-218) or zero
-      if (in_units && t.k != INT_MAX) {
-        const int sh = (E - 52) - t.k;
-        unsigned long long a = 0;
-        bool tie = false, fits = true;
-        if (sh <= 0) {
-          fits = sh > -54 && (t.M >> (54 + sh)) == 0;
-          a = fits ? t.M << -sh : 0;
-        } else if (sh < 64) {
-          const unsigned long long rem = t.M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-          a = (t.M >> sh) + (rem > half ? 1ull : 0ull);
-          tie = rem == half;
+      uint8_t f = rb.flag[j];
+      if (!f) continue;  // skipped (metrics.rs:216-218) or zero
+      unsigned long long a = rb.a[j];
+      if (in_units && !(start_units && E == E0)) f = increment(term(rb.raw[j], scale, sq), E, a);
+      if (in_units && (f & 2) && u + a < kTwo53) {  // the exact sum stays below 2^(E+1): the binade's grid
+        u += (f & 4) ? (a + ((u + a) & 1ull)) : a;
+        if (u == kTwo53) {  // a tie rounded up to 2^(E+1): the next binade
+          u = 1ull << 52;
+          ++E;
         }
-        if (fits && u + a < kTwo53) {  // the exact sum stays below 2^(E+1): the grid is the binade's
-          u += tie ? (a + ((u + a) & 1ull)) : a;
-          if (u == kTwo53) {  // a tie rounded up to 2^(E+1): the next binade
-            u = 1ull << 52;
-            ++E;
-          }
-          continue;
-        }
-        acc = from_units(u, E);
+        continue;
       }
-      acc = __dadd_rn(acc, term_value(raw, scale, sq));  // metrics.rs:223-224
+      if (in_units) acc = from_units(u, E);
+      acc = __dadd_rn(acc, term_value(rb.raw[j], scale, sq));  // metrics.rs:223-224
       in_units = isfinite(acc) && acc > 0.0;
       if (in_units) {
         E = binade_of(acc);
@@ -548,14 +580,51 @@ __device__ void replay_chunk(const float* __restrict__ map, long long n, float s
   __syncwarp();
 }
 
+// Largest total of aggregate-level entries the walker keeps in shared memory.
+constexpr size_t kWalkSmemBytes = 96 * 1024;
+constexpr int kEntryBytes = 20;  // i0, i1, meta
+
+// The lowest level (>= 1) from which all levels fit kWalkSmemBytes.
+__host__ __device__ __forceinline__ int cached_from(const long long* cnt, int nlev) {
+  long long bytes = 0;
+  int L = nlev;
+  while (L - 1 >= 1 && bytes + cnt[L - 1] * kEntryBytes <= (long long)kWalkSmemBytes) {
+    --L;
+    bytes += cnt[L] * kEntryBytes;
+  }
+  return L;
+}
+
 // 5. The walker: block 0 follows the sum of values, block 1 the sum of squares.
+// The small aggregate levels are copied to shared memory first, so that the
+// walker's level probes near a crossing cost shared-memory latency; level 0
+// (and level 1 when large) stay in global memory.
 __global__ void __launch_bounds__(32) osum_walk_kernel(const float* __restrict__ map, long long n, float scale,
                                                        Walk ws, Walk wq, double* __restrict__ out) {
-  __shared__ float buf[kChunk];
+  extern __shared__ __align__(16) unsigned char walk_smem[];
+  __shared__ ReplayBuf rb;
   const bool sq = blockIdx.x == 1;
-  const Walk& W = sq ? wq : ws;
+  Walk W = sq ? wq : ws;
   const int lane = threadIdx.x;
   const long long nchunks = W.cnt[0];
+  {
+    const int Lc = cached_from(W.cnt, W.nlev);
+    unsigned char* p = walk_smem;
+    for (int L = Lc; L < W.nlev; ++L) {
+      const long long c = W.cnt[L];
+      unsigned long long* i0 = reinterpret_cast<unsigned long long*>(p);
+      unsigned long long* i1 = i0 + c;
+      uint32_t* meta = reinterpret_cast<uint32_t*>(i1 + c);
+      for (long long i = lane; i < c; i += 32) {
+        i0[i] = W.lv[L].i0[i];
+        i1[i] = W.lv[L].i1[i];
+        meta[i] = W.lv[L].meta[i];
+      }
+      W.lv[L] = Level{i0, i1, meta};
+      p += ((size_t)c * kEntryBytes + 15) & ~(size_t)15;
+    }
+    __syncwarp();
+  }
   double s = 0.0;
   long long c = 0;
   while (c < nchunks) {
@@ -601,7 +670,7 @@ __global__ void __launch_bounds__(32) osum_walk_kernel(const float* __restrict__
       }
     }
     if (!moved) {
-      replay_chunk(map, n, scale, sq, c, s, lane, buf);
+      replay_chunk(map, n, scale, sq, c, s, lane, rb);
       ++c;
     }
   }
@@ -647,8 +716,8 @@ cudaError_t launch_ordered_sums(const float* map, long long n, float scale, cons
   };
   float* cs = reinterpret_cast<float*>(take((size_t)nchunks * 4));
   float* cq = reinterpret_cast<float*>(take((size_t)nchunks * 4));
-  double* bs = reinterpret_cast<double*>(take((size_t)nblocks * 8));
-  double* bq = reinterpret_cast<double*>(take((size_t)nblocks * 8));
+  unsigned long long* bs = reinterpret_cast<unsigned long long*>(take((size_t)nblocks * 8));
+  unsigned long long* bq = reinterpret_cast<unsigned long long*>(take((size_t)nblocks * 8));
   Walk ws{}, wq{};
   long long cnt[kMaxLevels];
   const int nlev = level_counts(nchunks, cnt);
@@ -673,7 +742,13 @@ cudaError_t launch_ordered_sums(const float* map, long long n, float scale, cons
     osum_level_kernel<<<g, 32 * warps_per_cta, 0, s>>>(ws.lv[L - 1], wq.lv[L - 1], cnt[L - 1], ws.lv[L], wq.lv[L]);
     ++*launches;
   }
-  osum_walk_kernel<<<2, 32, 0, s>>>(map, n, scale, ws, wq, out);
+  const int Lc = cached_from(cnt, nlev);
+  size_t wsmem = 0;
+  for (int L = Lc; L < nlev; ++L) wsmem += ((size_t)cnt[L] * kEntryBytes + 15) & ~(size_t)15;
+  cudaError_t e = cudaFuncSetAttribute(osum_walk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kWalkSmemBytes + 1024);
+  if (e != cudaSuccess) return e;
+  osum_walk_kernel<<<2, 32, wsmem, s>>>(map, n, scale, ws, wq, out);
   ++*launches;
   return cudaGetLastError();
 }
