@@ -20,11 +20,11 @@ At N = 1 the extras add the 1024^3 plate specimen (the same legs), the
 oracle, OpenMP over all host cores; the Rust reference cannot be built here)
 on the whole specimen of the workload, every step.
 --profile-case N: a small case for profilers with a kernel filter (no timing):
-one Tb.Th local thickness of a seeded N^3 specimen as warm-up (tables built),
-then Tb.Th and Tb.Sp again -- the launches worth capturing.  The specimen is
-the 512^3 workload's generator at edge N (sigma 5, BV/TV 0.15, cylinder ROI of
-radius 0.47 N); with --plates the 1024^3 workload's (sigma (4, 4, 8), BV/TV
-0.30, sphere ROI of radius 500 N / 1024).
+Tb.Th and Tb.Sp of a seeded N^3 specimen twice, phases one after the other --
+the first call is the warm-up (tables built), the second holds the launches
+worth capturing.  The specimen is the 512^3 workload's generator at edge N
+(sigma 5, BV/TV 0.15, cylinder ROI of radius 0.47 N); with --plates the 1024^3
+workload's (sigma (4, 4, 8), BV/TV 0.30, sphere ROI of radius 500 N / 1024).
 
 Multi-process (torchrun): every rank processes its own specimen (different
 seed, same shape) with no data exchange -- replicas, weak scaling; rank 0
@@ -642,11 +642,13 @@ def run_gpu(args, rank, world, local):
 
 
 def run_profile_case(args) -> int:
-    """A small case for profilers with a kernel filter (no timing, no JSON line)."""
-    import numpy as np
+    """A small case for profilers with a kernel filter (no timing, no JSON line):
+    Tb.Th and Tb.Sp of one specimen twice (the first call builds the tables and
+    grows the buffers; the second holds the launches worth capturing), the
+    phases one after the other so that each kernel runs alone."""
     import torch
 
-    from bone_morphometry_gb300 import Context, Phase, local_thickness
+    from bone_morphometry_gb300 import Context, analyze_thickness
     from bone_morphometry_gb300 import synthetic as S
 
     n = args.profile_case
@@ -656,11 +658,11 @@ def run_profile_case(args) -> int:
     else:
         sp = S.make_specimen((n, n, n), 5.0, 0.15, "cylinder", 0.47 * n, 19.5, 1002)
     ctx = Context(0)
-    th = torch.from_numpy(((sp.roi != 0) & (sp.bone != 0)).astype(np.uint8)).cuda()
-    ma = torch.from_numpy(((sp.roi != 0) & (sp.bone == 0)).astype(np.uint8)).cuda()
-    local_thickness(th, Phase.FOREGROUND, ctx=ctx)
-    local_thickness(th, Phase.FOREGROUND, ctx=ctx)
-    local_thickness(ma, Phase.FOREGROUND, ctx=ctx)
+    ctx.set_concurrent_phases(False)
+    bone = torch.from_numpy(sp.bone).cuda()
+    roi = torch.from_numpy(sp.roi).cuda()
+    for _ in range(2):
+        analyze_thickness(bone, roi, sp.spacing_um, ctx=ctx)
     torch.cuda.synchronize()
     ctx.close()
     print("profile case done: %d^3%s" % (n, " plates" if args.plates else ""))

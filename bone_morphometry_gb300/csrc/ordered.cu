@@ -633,9 +633,10 @@ __global__ void __launch_bounds__(32) osum_walk_kernel(const float* __restrict__
     // before the first value (s = 0) only empty runs, after it runs in s's binade
     bool moved = false;
     for (int L = W.nlev - 1; L >= 0 && !moved; --L) {
-      const long long span = 1ll << (5 * L);
-      if (c % span) continue;
-      const long long q = c / span;
+      const int lg = 5 * L;
+      const long long span = 1ll << lg;
+      if (c & (span - 1)) continue;
+      const long long q = c >> lg;
       // up to 32 entries of this level, but not past the next block of level L + 1
       const long long lim = (L + 1 < W.nlev) ? ((q / 32) + 1) * 32 : W.cnt[L];
       const long long qe = lim < W.cnt[L] ? lim : W.cnt[L];
