@@ -222,21 +222,17 @@ __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uin
   }
 }
 
-// Half-word index of voxel (row, x) in the u16 value array: pairs of x share a
-// 32-bit word; the word is XOR-swizzled by the row so that threads touching the
-// same x of different rows fall into different banks.
-__device__ __forceinline__ int vidx(int row, int x) {
-  return row * 32 + (((((x >> 1) ^ (row & 15)) << 1)) | (x & 1));
-}
-
-constexpr size_t kTileFillSmemWords = (size_t)kRows * 16 + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
+constexpr size_t kTileFillSmemWords = (size_t)kRows + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
                                       (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130 +
                                       (kHxMax + 1) * kHxStride / 4;
 
 // One CTA per tile (32 x 32 x 16 voxels) paints the tile's selected voxels.
+// A painted voxel's r^2 goes straight to the map (each selected voxel is
+// painted once: its bit in usel is cleared atomically first), and the voxels
+// left unpainted get 0 at the end; without a per-voxel value array the CTA
+// needs 26 KB of shared memory, and 5 CTAs share an SM (48 registers).
 // Shared memory:
-//   val  : u16 per voxel, 0 = unpainted, else 1 + rank of the r^2 painted
-//          (rank 0 = largest r^2 present);
+//   sown : per row (z, y), the tile's selected voxels;
 //   usel : per row (z, y), the selected voxels not yet painted;
 //   boff / nzb : the tile's bin offsets and the list of non-empty bins for
 //          the current chunk of bins;
@@ -255,16 +251,16 @@ constexpr size_t kTileFillSmemWords = (size_t)kRows * 16 + kRows + (kBinChunk + 
 // 1 to 8 threads per item (more when the round has few items) walks the
 // disk's rows and paints each row's chord of unpainted voxels.  Balls of one
 // bin have the same r^2, so the order of their items does not matter (two
-// threads may write the same tag).  Non-selected voxels are left 0 here;
+// threads may write the same value).  Non-selected voxels are left 0 here;
 // the site pass or the chain passes add the ones a sphere reaches.
-__global__ void __launch_bounds__(kFillThreads, 4)
+__global__ void __launch_bounds__(kFillThreads, 5)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
                  const uint32_t* __restrict__ rvals, const uint4* __restrict__ rgeo, const FillInfo* __restrict__ info,
                  const uint32_t* __restrict__ selbits, Dims dm, VoxelDecoder vd, Geom g,
                  const uint32_t* __restrict__ order, uint32_t* __restrict__ fillmap) {
   extern __shared__ uint32_t smem[];
-  uint16_t* val = reinterpret_cast<uint16_t*>(smem);       // kRows * 32 half-words
-  uint32_t* usel = smem + kRows * 16;                        // kRows
+  uint32_t* sown = smem;                                     // kRows: the tile's selected voxels per row
+  uint32_t* usel = smem + kRows;                             // kRows
   uint32_t* boff = usel + kRows;                             // kBinChunk + 1
   uint32_t* nzb = boff + kBinChunk + 4;                      // kBinChunk
   uint32_t* ent = nzb + kBinChunk;                           // kEntWin
@@ -299,7 +295,6 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       }
       continue;
     }
-    for (int i = tid; i < kRows * 16; i += kFillThreads) smem[i] = 0u;
     if (tid == 0) {
       s_wlo = 0u;
       s_whi = 0u;
@@ -313,6 +308,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       uint32_t own = 0u;
       if (zz < vz && yy < vy) own = selbits[((long long)(z0 + zz) * dm.h + (y0 + yy)) * nw + tx] & xmask;
       usel[urow(zz, yy)] = own;
+      sown[urow(zz, yy)] = own;
       any_sel = any_sel || own != 0u;
     }
     if (!__syncthreads_or(any_sel)) {  // nothing selected here (outside the ROI, say): all zero
@@ -353,7 +349,6 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
         const uint32_t bl = nzb[k];
         const uint4 gq = rgeo[b0 + bl];
         const int R = (int)gq.x;
-        const uint16_t tag = (uint16_t)(b0 + bl + 1u);
         const int rad = (int)gq.z;                         // isqrt(r2): no lattice point of the ball is further
         const uint32_t e = boff[bl + 1];
         // this bin's disk radii: hyt[|dz|] = isqrt(r2 - dz^2); for small balls
@@ -460,10 +455,10 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
               uint32_t bits = m & range_mask(xa, xb);
               if (!bits) continue;
               atomicAnd(&usel[row], ~bits);
-              const int vrow = zz * kFillTY + y;
+              // every selected voxel is painted once (its bit cleared above): straight to the map
+              uint32_t* orow = fillmap + ((long long)(z0 + zz) * dm.h + (y0 + y)) * dm.w + x0;
               while (bits) {
-                const int xx = __ffs(bits) - 1;
-                val[vidx(vrow, xx)] = tag;
+                orow[__ffs(bits) - 1] = (uint32_t)R;
                 bits &= bits - 1u;
               }
             }
@@ -475,13 +470,13 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
       }
     }
     __syncthreads();
-    // write the tile: one 128-byte row per warp step, rank -> r^2
+    // the voxels no ball painted (non-selected ones; the site pass adds those
+    // a sphere reaches) get 0: one row per warp step
     for (int r = warp; r < kRows; r += kFillWarps) {
       const int zz = r / kFillTY, yy = r % kFillTY;
-      if (zz < vz && yy < vy && lane < vx) {
-        const uint32_t t = val[vidx(r, lane)];
-        fillmap[((long long)(z0 + zz) * dm.h + (y0 + yy)) * dm.w + x0 + lane] = t ? rvals[t - 1u] : 0u;
-      }
+      const uint32_t painted = sown[urow(zz, yy)] & ~usel[urow(zz, yy)];
+      if (zz < vz && yy < vy && lane < vx && !((painted >> lane) & 1u))
+        fillmap[((long long)(z0 + zz) * dm.h + (y0 + yy)) * dm.w + x0 + lane] = 0u;
     }
     __syncthreads();
   }
