@@ -33,10 +33,11 @@
 //      skips empty runs before the first value, applies the largest aligned
 //      run whose predicted binade is the one s is in and whose result stays
 //      in it (32 entries of a level at a time, composed by a warp
-//      reduction), and replays a chunk value by value -- integer increments
-//      of s/U, and a hardware f64 addition, the reference's own operation,
-//      for a value that leaves the binade -- where no prediction holds: at
-//      the ~30 binade crossings of each sum.
+//      reduction), and replays a chunk where no prediction holds -- at the
+//      ~30 binade crossings of each sum: lanes fold their values, a warp
+//      scan finds the lane whose values leave the binade, and that lane adds
+//      them one by one (integer increments of s/U, and a hardware f64
+//      addition, the reference's own operation, for the value that crosses).
 // Every step the walker takes is checked against the exact state, so a wrong
 // prediction costs time, never exactness.  No per-value f64 arithmetic: the
 // GB300's f64 rate is a small fraction of its f32 and integer rates.  Not a
@@ -498,86 +499,125 @@ struct Walk {
   int nlev;
 };
 
-// Replays chunk c from state s as the reference adds, value after value.  s
-// is kept as an integer count u of its binade's ulps; every value's rounded
-// increment a (and whether it is a tie) for the binade s starts the chunk in
-// is computed by the warp in parallel, then lane 0 adds them in order (round
-// half to even on u for a tie) and falls back to a hardware f64 addition --
-// the reference's own operation -- for the first value (s = 0), for a value
-// that leaves the binade, and for +inf; after such a change of binade it
-// computes the remaining increments itself.  s is broadcast back.
-struct ReplayBuf {
-  unsigned long long a[kChunk];
-  float raw[kChunk];
-  uint8_t flag[kChunk];  // 0: skipped; bit 0: value; bit 1: a fits the binade; bit 2: tie
-};
-
-__device__ __forceinline__ uint8_t increment(const Term& t, int E, unsigned long long& a) {
-  if (!t.M) return 0;
-  if (t.k == INT_MAX) {
-    a = 0;
-    return 1;  // +inf: f64 path
-  }
-  const int sh = (E - 52) - t.k;
-  a = 0;
-  if (sh <= 0) {
-    const bool fits = sh > -54 && (t.M >> (54 + sh)) == 0;
-    a = fits ? t.M << -sh : 0;
-    return fits ? 3 : 1;
-  }
-  if (sh < 64) {
-    const unsigned long long rem = t.M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-    a = (t.M >> sh) + (rem > half ? 1ull : 0ull);
-    return rem == half ? 7 : 3;
-  }
-  return 3;  // far below half an ulp: a = 0
-}
-
-__device__ void replay_chunk(const float* __restrict__ map, long long n, float scale, bool sq, long long c, double& s,
-                             int lane, ReplayBuf& rb) {
-  const bool start_units = isfinite(s) && s > 0.0;
-  const int E0 = start_units ? binade_of(s) : 0;
-  for (int j = lane; j < kChunk; j += 32) {
-    const long long idx = c * kChunk + j;
-    const float raw = idx < n ? map[idx] : 0.0f;
-    const Term t = term(raw, scale, sq);
-    unsigned long long a = 0;
-    rb.raw[j] = raw;
-    rb.flag[j] = start_units ? increment(t, E0, a) : (t.M ? 1 : 0);
-    rb.a[j] = a;
-  }
-  __syncwarp();
-  if (lane == 0) {
-    double acc = s;
-    bool in_units = start_units;  // u / E hold acc
-    int E = E0;
-    unsigned long long u = start_units ? units_of(acc) : 0ull;
-    for (int j = 0; j < kChunk; ++j) {
-      uint8_t f = rb.flag[j];
-      if (!f) continue;  // skipped (metrics.rs:216-218) or zero
-      unsigned long long a = rb.a[j];
-      if (in_units && !(start_units && E == E0)) f = increment(term(rb.raw[j], scale, sq), E, a);
-      if (in_units && (f & 2) && u + a < kTwo53) {  // the exact sum stays below 2^(E+1): the binade's grid
-        u += (f & 4) ? (a + ((u + a) & 1ull)) : a;
+// Adds values vals[j0 .. 8) to s one after the other as the reference does
+// (one thread): s kept as an integer count of its binade's ulps plus each
+// value's rounded increment (round half to even on that count), a hardware
+// f64 addition -- the reference's own operation -- for the first value
+// (s = 0), for a value that leaves the binade, and for +inf.
+__device__ double add_serially(double s, const float (&vals)[8], int j0, float scale, bool sq) {
+  bool in_units = isfinite(s) && s > 0.0;
+  int E = in_units ? binade_of(s) : 0;
+  unsigned long long u = in_units ? units_of(s) : 0ull;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if (j < j0) continue;
+    const Term t = term(vals[j], scale, sq);
+    if (!t.M) continue;  // skipped (metrics.rs:216-218) or zero
+    if (in_units && t.k != INT_MAX) {
+      const int sh = (E - 52) - t.k;
+      unsigned long long a = 0;
+      bool tie = false, fits = true;
+      if (sh <= 0) {
+        fits = sh > -54 && (t.M >> (54 + sh)) == 0;
+        a = fits ? t.M << -sh : 0;
+      } else if (sh < 64) {
+        const unsigned long long rem = t.M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        a = (t.M >> sh) + (rem > half ? 1ull : 0ull);
+        tie = rem == half;
+      }
+      if (fits && u + a < kTwo53) {  // the exact sum stays below 2^(E+1): the binade's grid
+        u += tie ? (a + ((u + a) & 1ull)) : a;
         if (u == kTwo53) {  // a tie rounded up to 2^(E+1): the next binade
           u = 1ull << 52;
           ++E;
         }
         continue;
       }
-      if (in_units) acc = from_units(u, E);
-      acc = __dadd_rn(acc, term_value(rb.raw[j], scale, sq));  // metrics.rs:223-224
-      in_units = isfinite(acc) && acc > 0.0;
-      if (in_units) {
-        E = binade_of(acc);
-        u = units_of(acc);
-      }
+      s = from_units(u, E);
     }
-    if (in_units) acc = from_units(u, E);
-    s = acc;
+    s = __dadd_rn(s, term_value(vals[j], scale, sq));  // metrics.rs:223-224
+    in_units = isfinite(s) && s > 0.0;
+    if (in_units) {
+      E = binade_of(s);
+      u = units_of(s);
+    }
+  }
+  return in_units ? from_units(u, E) : s;
+}
+
+__device__ __forceinline__ Fn shfl_up_fn(const Fn& f, int o) {
+  Fn r;
+  r.i0 = __shfl_up_sync(0xffffffffu, f.i0, o);
+  r.i1 = __shfl_up_sync(0xffffffffu, f.i1, o);
+  r.meta = __shfl_up_sync(0xffffffffu, f.meta, o);
+  return r;
+}
+
+// Inclusive in-order scan: lane j gets the composition of lanes 0 .. j.
+__device__ __forceinline__ Fn warp_scan_fn(Fn f, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const Fn g = shfl_up_fn(f, o);
+    if (lane >= o) f = compose(g, f);
+  }
+  return f;
+}
+
+// Replays chunk c from state s exactly as the reference adds.  Lane l holds
+// values 8l .. 8l+7.  In s's binade every lane folds its values into one
+// function and a warp scan composes them in order; the first lane whose
+// prefix leaves the binade (or the lane holding the first value, s = 0)
+// adds its values serially with add_serially, and the lanes after it are
+// folded again in the new binade.  s is broadcast back.
+__device__ void replay_chunk(const float* __restrict__ map, long long n, float scale, bool sq, long long c, double& s,
+                             int lane) {
+  float vals[8];
+  load8(map, n, c * kChunk + lane * 8, vals);
+  int start = 0;  // first lane not yet added
+  const int mbits = sq ? 48 : 24;
+  while (start < 32) {
+    if (!isfinite(s)) break;  // +inf stays +inf
+    int b;                    // the lane that adds serially
+    if (s == 0.0) {
+      bool any = false;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) any = any || term(vals[j], scale, sq).M != 0;
+      const unsigned m = __ballot_sync(0xffffffffu, lane >= start && any);
+      if (!m) break;
+      b = __ffs(m) - 1;
+    } else {
+      const int E = binade_of(s);
+      const unsigned long long u0 = units_of(s);
+      Acc A{0ull, 0ull, 0u, 1u};
+      bool any = false;
+      if (lane >= start) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const Term t = term(vals[j], scale, sq);
+          if (t.M) {
+            any = true;
+            acc_elem(A, t.M, t.k, E - 52, mbits);
+          }
+        }
+      }
+      const Fn pre = warp_scan_fn(acc_fn(A, any, E), lane);
+      const unsigned long long after = sat_add(u0, (u0 & 1ull) ? pre.i1 : pre.i0);
+      const unsigned bad = __ballot_sync(0xffffffffu, lane >= start && after > kTwo53);
+      if (!bad) {
+        s = from_units(__shfl_sync(0xffffffffu, after, 31), E);
+        break;
+      }
+      b = __ffs(bad) - 1;
+      // lanes start .. b-1 stay in the binade: s after them
+      const unsigned long long ub = __shfl_sync(0xffffffffu, after, b > 0 ? b - 1 : 0);
+      if (b > start) s = from_units(ub, E);
+    }
+    double sb = 0.0;
+    if (lane == b) sb = add_serially(s, vals, 0, scale, sq);
+    s = __shfl_sync(0xffffffffu, sb, b);
+    start = b + 1;
   }
   s = __shfl_sync(0xffffffffu, s, 0);
-  __syncwarp();
 }
 
 // Largest total of aggregate-level entries the walker keeps in shared memory.
@@ -602,7 +642,6 @@ __host__ __device__ __forceinline__ int cached_from(const long long* cnt, int nl
 __global__ void __launch_bounds__(32) osum_walk_kernel(const float* __restrict__ map, long long n, float scale,
                                                        Walk ws, Walk wq, double* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char walk_smem[];
-  __shared__ ReplayBuf rb;
   const bool sq = blockIdx.x == 1;
   Walk W = sq ? wq : ws;
   const int lane = threadIdx.x;
@@ -671,7 +710,7 @@ __global__ void __launch_bounds__(32) osum_walk_kernel(const float* __restrict__
       }
     }
     if (!moved) {
-      replay_chunk(map, n, scale, sq, c, s, lane, rb);
+      replay_chunk(map, n, scale, sq, c, s, lane);
       ++c;
     }
   }
