@@ -201,9 +201,7 @@ constexpr int kEntWin = 768;      // ball entries staged in shared memory at a t
 constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself)
 constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
 constexpr int kRotStride = 33;    // words per range-OR row: lanes testing different planes hit different banks
-constexpr int kItems = 1024;      // (ball, plane) paint items per round
-constexpr int kHxMax = 31;        // balls up to this radius read their chord half-widths from a table
-constexpr int kHxStride = 36;     // bytes per |dz| row of that table (9 words: consecutive planes, other banks)
+constexpr int kItems = 4096;      // (ball, plane) paint items per round
 constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
 
 // rot[lv - 1][z][y] (rows of kRotStride words) = OR of the unpainted-voxel
@@ -223,14 +221,13 @@ __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uin
 }
 
 constexpr size_t kTileFillSmemWords = (size_t)kRows + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
-                                      (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130 +
-                                      (kHxMax + 1) * kHxStride / 4;
+                                      (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130;
 
 // One CTA per tile (32 x 32 x 16 voxels) paints the tile's selected voxels.
 // A painted voxel's r^2 goes straight to the map (each selected voxel is
 // painted once: its bit in usel is cleared atomically first), and the voxels
 // left unpainted get 0 at the end; without a per-voxel value array the CTA
-// needs 26 KB of shared memory, and 5 CTAs share an SM (48 registers).
+// needs 39 KB of shared memory, and 5 CTAs share an SM (48 registers).
 // Shared memory:
 //   sown : per row (z, y), the tile's selected voxels;
 //   usel : per row (z, y), the selected voxels not yet painted;
@@ -267,10 +264,10 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
   uint32_t* rot = ent + kEntWin;                             // (kRotLevels - 1) * kFillTZ * kRotStride
   uint32_t* item = rot + (kRotLevels - 1) * kFillTZ * kRotStride;  // kItems
   uint16_t* hyt = reinterpret_cast<uint16_t*>(item + kItems);              // 257 (+1) half-words
-  uint8_t* hxt = reinterpret_cast<uint8_t*>(item + kItems + 130);         // (kHxMax + 1) * kHxStride bytes
   __shared__ uint32_t s_nnz, s_wlo, s_whi;
   __shared__ uint32_t s_nitem[2];
   __shared__ uint32_t wcnt[kFillWarps];
+  __shared__ uint2 sgeo[kBinChunk];  // (r2, isqrt(r2)) of the chunk's non-empty bins
   const uint32_t nR = info->nR;
   const int nw = dm.nw();
   const int tid = threadIdx.x;
@@ -345,22 +342,19 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
         __syncthreads();
       }
       const uint32_t nnz = s_nnz;
+      for (uint32_t i = tid; i < nnz; i += kFillThreads) {
+        const uint4 q = rgeo[b0 + nzb[i]];
+        sgeo[i] = make_uint2(q.x, q.z);
+      }
+      __syncthreads();
       for (uint32_t k = 0; k < nnz; ++k) {
         const uint32_t bl = nzb[k];
-        const uint4 gq = rgeo[b0 + bl];
+        const uint2 gq = sgeo[k];
         const int R = (int)gq.x;
-        const int rad = (int)gq.z;                         // isqrt(r2): no lattice point of the ball is further
+        const int rad = (int)gq.y;                         // isqrt(r2): no lattice point of the ball is further
         const uint32_t e = boff[bl + 1];
-        // this bin's disk radii: hyt[|dz|] = isqrt(r2 - dz^2); for small balls
-        // also the chord half-widths hxt[|dz| * kHxStride + |dy|] = isqrt(r2 - dz^2 - dy^2)
+        // this bin's disk radii: hyt[|dz|] = isqrt(r2 - dz^2)
         for (int i = tid; i <= rad; i += kFillThreads) hyt[i] = (uint16_t)isqrt24((uint32_t)(R - i * i));
-        if (rad <= kHxMax) {
-          for (int i = tid; i < (rad + 1) * 32; i += kFillThreads) {
-            const int a = i >> 5, c = i & 31;
-            const int t = R - a * a - c * c;
-            hxt[a * kHxStride + c] = t >= 0 ? (uint8_t)isqrt24((uint32_t)t) : (uint8_t)0;
-          }
-        }
         if (k % kRotEvery == 0 && k > 0) build_rot(usel, rot, warp, lane, kFillWarps);
         __syncthreads();
         for (uint32_t ss = boff[bl]; ss < e;) {
@@ -441,15 +435,18 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             const int bx = (int)(cb & 0x3ffu) - 512, by = (int)((cb >> 10) & 0x3ffu) - 512;
             const int dz = zz - ((int)(cb >> 20) - 512);
             const int rz = R - dz * dz;
-            const uint8_t* hxz = hxt + abs(dz) * kHxStride;
+            // rows whose unpainted voxels all lie outside the disk's widest chord are skipped
+            // before the row's own chord is computed
+            const int hw = (int)hyt[abs(dz)];
+            const uint32_t wide = range_mask(max(bx - hw, 0), min(bx + hw, vx - 1));
             for (int y = ya + sub; y <= yb; y += G) {
               const int row = urow(zz, y);
-              const uint32_t m = usel[row];
+              const uint32_t m = usel[row] & wide;
               if (!m) continue;
               const int dy = y - by;
               const int t = rz - dy * dy;
               if (t < 0) continue;
-              const int hx = rad <= kHxMax ? (int)hxz[abs(dy)] : (int)isqrt24((uint32_t)t);
+              const int hx = (int)isqrt24((uint32_t)t);
               const int xa = max(bx - hx, 0), xb = min(bx + hx, vx - 1);
               if (xa > xb) continue;
               uint32_t bits = m & range_mask(xa, xb);
