@@ -119,7 +119,7 @@ struct FixedPartial {
 
 // Tile of the tile-owned sphere fill (x, y, z voxels).
 constexpr int kFillTX = 32;
-constexpr int kFillTY = 32;
+constexpr int kFillTY = 64;
 constexpr int kFillTZ = 16;
 
 // Largest r^2 whose sphere lattice points the tile fill tabulates (radius 256);

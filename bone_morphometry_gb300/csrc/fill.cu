@@ -4,7 +4,7 @@
 // sum over ridges of |ball| operations (~7e10 for a 512^3 marrow phase, where
 // every voxel is covered ~500 times).  Here the work splits in two:
 //
-// Selected voxels: the output volume is cut into 32x32x16 tiles, each owned by
+// Selected voxels: the output volume is cut into 32x64x16 tiles, each owned by
 // one CTA that paints its tile in shared memory.  The balls that reach a tile
 // are visited in strictly descending r^2 (a counting sort by (tile, r^2
 // rank)); the final value of a voxel is the r^2 of the first -- largest --
@@ -185,7 +185,7 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
 
 constexpr int kFillThreads = 256;
 constexpr int kFillWarps = kFillThreads / 32;
-constexpr int kRows = kFillTZ * kFillTY;  // 512 rows of 32 voxels per tile
+constexpr int kRows = kFillTZ * kFillTY;  // 1024 rows of 32 voxels per tile
 
 __device__ __forceinline__ uint32_t range_mask(int a, int b) {  // bits a..b, 0 <= a <= b <= 31
   return (0xffffffffu >> (31 - b)) & (0xffffffffu << a);
@@ -198,24 +198,35 @@ __device__ __forceinline__ int urow(int z, int y) { return z * kFillTY + ((y + 3
 
 constexpr int kBinChunk = 256;    // bins whose offsets are staged in shared memory at a time
 constexpr int kEntWin = 768;      // ball entries staged in shared memory at a time
-constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself)
+constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself);
+                                  // two 32-row lookups cover a plane's 64 rows
 constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
-constexpr int kRotStride = 33;    // words per range-OR row: lanes testing different planes hit different banks
-constexpr int kItems = 4096;      // (ball, plane) paint items per round
+constexpr int kRotStride = 65;    // words per range-OR row: lanes testing different planes hit different banks
+constexpr int kItems = 2048;      // (ball, plane) paint items per round
 constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
+// a paint item packs (window index << 16) | (rows - 1) << 10 | first row << 4 | plane
+static_assert(kEntWin <= (1 << 16) && kFillTY <= 64 && kFillTZ <= 16, "paint item encoding");
 
 // rot[lv - 1][z][y] (rows of kRotStride words) = OR of the unpainted-voxel
 // masks of rows y .. y + 2^lv - 1 of plane z (rows past the tile edge count
-// as empty), lv = 1 .. 5.  Built with shuffles, one plane per warp step.
+// as empty), lv = 1 .. 5.  Built with shuffles, one plane per warp step; lane
+// l holds rows l and l + 32.
 __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uint32_t* __restrict__ rot, int warp,
                                           int lane, int nwarps) {
+  static_assert(kFillTY == 64, "two rows per lane");
   for (int zz = warp; zz < kFillTZ; zz += nwarps) {
-    uint32_t v = usel[urow(zz, lane)];
+    uint32_t v0 = usel[urow(zz, lane)], v1 = usel[urow(zz, lane + 32)];
 #pragma unroll
     for (int lv = 1; lv < kRotLevels; ++lv) {
-      const uint32_t u = __shfl_down_sync(0xffffffffu, v, 1 << (lv - 1));
-      v |= (lane + (1 << (lv - 1)) < 32) ? u : 0u;
-      rot[((lv - 1) * kFillTZ + zz) * kRotStride + lane] = v;
+      const int s = 1 << (lv - 1);  // row y takes the previous level's rows y and y + s
+      const uint32_t a = __shfl_sync(0xffffffffu, v0, (lane + s) & 31);
+      const uint32_t b = __shfl_sync(0xffffffffu, v1, (lane + s) & 31);
+      const bool lo = lane + s < 32;
+      v0 |= lo ? a : b;
+      v1 |= lo ? b : 0u;
+      uint32_t* rr = rot + ((lv - 1) * kFillTZ + zz) * kRotStride;
+      rr[lane] = v0;
+      rr[lane + 32] = v1;
     }
   }
 }
@@ -223,11 +234,11 @@ __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uin
 constexpr size_t kTileFillSmemWords = (size_t)kRows + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
                                       (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130;
 
-// One CTA per tile (32 x 32 x 16 voxels) paints the tile's selected voxels.
+// One CTA per tile (32 x 64 x 16 voxels) paints the tile's selected voxels.
 // A painted voxel's r^2 goes straight to the map (each selected voxel is
 // painted once: its bit in usel is cleared atomically first), and the voxels
 // left unpainted get 0 at the end; without a per-voxel value array the CTA
-// needs 39 KB of shared memory, and 5 CTAs share an SM (48 registers).
+// needs 44 KB of shared memory, and 5 CTAs share an SM (48 registers).
 // Shared memory:
 //   sown : per row (z, y), the tile's selected voxels;
 //   usel : per row (z, y), the selected voxels not yet painted;
@@ -393,8 +404,8 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             const int xa = max(cx - hy, 0), xb = min(cx + hy, vx - 1);
             ok = ok && pya <= pyb && xa <= xb;
             const int zc = min(zz, kFillTZ - 1);
-            const int ya = min(pya, 31), yb = max(min(pyb, 31), ya);
-            const int lv = 31 - __clz(yb - ya + 1);  // 2^lv <= span
+            const int ya = min(pya, kFillTY - 1), yb = max(min(pyb, kFillTY - 1), ya);
+            const int lv = min(31 - __clz(yb - ya + 1), kRotLevels - 1);  // 2^lv <= span: two lookups cover it
             const uint32_t* tl = rot + (max(lv - 1, 0) * kFillTZ + zc) * kRotStride;
             const uint32_t orr = lv == 0 ? usel[urow(zc, ya)] : (tl[ya] | tl[yb - (1 << lv) + 1]);
             return ok && (orr & range_mask(min(max(xa, 0), 31), max(min(xb, 31), min(max(xa, 0), 31)))) != 0u;
@@ -408,7 +419,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
               base = __shfl_sync(0xffffffffu, base, 0);
               if (pass)
                 item[base + __popc(act & lanes_below)] =
-                    ((wb + bi) << 14) | ((uint32_t)(pyb - pya) << 9) | ((uint32_t)pya << 4) | (uint32_t)zz;
+                    ((wb + bi) << 16) | ((uint32_t)(pyb - pya) << 10) | ((uint32_t)pya << 4) | (uint32_t)zz;
             }
           };
           for (uint32_t bp = 4 * warp; bp < se - ss; bp += 4 * kFillWarps) {
@@ -430,8 +441,8 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
           const int G = 1 << lg, sub = tid & (G - 1);
           for (uint32_t it = (uint32_t)(tid >> lg); it < nitem; it += (uint32_t)(kFillThreads >> lg)) {
             const uint32_t q = item[it];
-            const int zz = (int)(q & 15u), ya = (int)((q >> 4) & 31u), yb = ya + (int)((q >> 9) & 31u);
-            const uint32_t cb = ent[q >> 14];
+            const int zz = (int)(q & 15u), ya = (int)((q >> 4) & 63u), yb = ya + (int)((q >> 10) & 63u);
+            const uint32_t cb = ent[q >> 16];
             const int bx = (int)(cb & 0x3ffu) - 512, by = (int)((cb >> 10) & 0x3ffu) - 512;
             const int dz = zz - ((int)(cb >> 20) - 512);
             const int rz = R - dz * dz;
