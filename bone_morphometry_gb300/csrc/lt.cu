@@ -110,19 +110,21 @@ __device__ constexpr signed char kN26c[26][3] = {
 
 // Fused surface cleanup (local_thickness.rs:210-281), phase mask (:31-43),
 // f32 calibration and exact moment sums (metrics.rs:215-226) on a tile of
-// 32 x 8 x 8 voxels.  The r^2 map is staged with a halo of 2 (out-of-volume
+// 32 x 16 x 8 voxels (the staged halo is 2.1 times the tile; 2.5 times at
+// 32 x 8 x 8).  The r^2 map is staged with a halo of 2 (out-of-volume
 // voxels hold kOob, which is neither zero nor interior -- look() returns -1
 // there).  Pass 1 ("nonzero and no zero 26-neighbour") is a 3x3x3 erosion of
 // the nonzero mask, done on 64-bit row masks (x, then y, then z); pass 2 sums
 // the diameters of interior neighbours in NEIGHBORS_26 order with IEEE f32
 // adds and one IEEE division, exactly as the reference.
-constexpr int kCTX = 32, kCTY = 8, kCTZ = 8;
+constexpr int kCTX = 32, kCTY = 16, kCTZ = 8;
 constexpr int kCH = 2;                       // halo
 constexpr int kCSX = kCTX + 2 * kCH;         // 36
-constexpr int kCSY = kCTY + 2 * kCH;         // 12
+constexpr int kCSY = kCTY + 2 * kCH;         // 20
 constexpr int kCSZ = kCTZ + 2 * kCH;         // 12
 constexpr uint32_t kOob = 0xffffffffu;
 constexpr int kCleanThreads = 256;
+static_assert(kCTZ * kCTY <= kCleanThreads, "the empty-tile check reads one selection word per thread");
 
 __device__ __forceinline__ void flush_run(StatsAccum& sacc, uint32_t e, unsigned long long& s1,
                                           unsigned long long& sh, unsigned long long& sl) {
@@ -225,7 +227,7 @@ cleanup_tile_kernel(const uint32_t* __restrict__ fm, const uint32_t* __restrict_
     // stage the r^2 map with halo 2: one row of 36 per warp step.  Each warp
     // has 18 rows; their loads are issued in batches of 3 before any use, so
     // the latencies overlap.
-    constexpr int kRowsPerWarp = kCSZ * kCSY / (kCleanThreads / 32);  // 18
+    constexpr int kRowsPerWarp = kCSZ * kCSY / (kCleanThreads / 32);  // 30
     constexpr int kBatch = 3;
     static_assert(kCSZ * kCSY % (kCleanThreads / 32) == 0 && kRowsPerWarp % kBatch == 0, "staging split");
 #pragma unroll
