@@ -315,28 +315,72 @@ void ordered_sums(bm_ctx* ctx, const float* d_map, long long n, float scale, con
   });
 }
 
+// The buffers of one phase's distance transform.
+struct EdtBufs {
+  uint32_t* A;        // x pass output (kept for the chain passes), y pass input
+  uint32_t* B;        // y pass output
+  void* scratch;      // envelope scratch of the flagged lines
+  uint32_t* selbits;  // selection bits
+  Counters* ctr;
+  uint8_t* redo;      // per-line flags of the windowed passes
+};
+
+EdtBufs edt_buffers(bm_ctx* ctx, Dims dm) {
+  const size_t N = (size_t)dm.n();
+  const size_t bits_bytes = (size_t)dm.nw() * dm.h * dm.d * sizeof(uint32_t);
+  EdtBufs b;
+  b.A = static_cast<uint32_t*>(ensure(ctx, ctx->dist, N * 4, "distance map"));
+  b.B = static_cast<uint32_t*>(ensure(ctx, ctx->dist2, N * 4, "distance map"));
+  b.scratch = ensure(ctx, ctx->stack, edt_scratch_bytes(dm), "envelope scratch");
+  b.selbits = static_cast<uint32_t*>(ensure(ctx, ctx->selbits, bits_bytes, "selection bits"));
+  b.ctr = static_cast<Counters*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
+  const size_t redo_bytes = (size_t)dm.w * (dm.h > dm.d ? dm.h : dm.d);
+  b.redo = static_cast<uint8_t*>(ensure(ctx, ctx->redo, redo_bytes, "line flags"));
+  return b;
+}
+
+// The x and y passes of planes z0 .. z1-1: both work within a plane, so a slab
+// of planes is a volume of its own (every offset is a whole number of planes,
+// which keeps the 16-byte alignment of rows whose width is a multiple of 4).
+// The counters accumulate over slabs.
+void edt_xy(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int mode, const EdtBufs& b, int z0, int z1,
+            cudaStream_t s) {
+  const Dims sd{dm.w, dm.h, z1 - z0};
+  const long long off = (long long)z0 * dm.w * dm.h;
+  const uint8_t* a = d_a + off;
+  const uint8_t* bb = d_b ? d_b + off : nullptr;
+  uint32_t* A = b.A + off;
+  uint32_t* B = b.B + off;
+  uint32_t* sel = b.selbits + (long long)z0 * dm.h * dm.nw();
+  timed(ctx, KF_EDT_X, s, "edt x pass",
+        [&] { return launch_edt_x(a, bb, mode, sd, A, sel, b.ctr, s, &ctx->launches); });
+  timed(ctx, KF_EDT_Y, s, "edt y pass", [&] {
+    return launch_edt_window(1, A, B, sd, b.scratch, b.redo, b.ctr, ctx->wait_cycles, s, &ctx->launches);
+  });
+}
+
 // One phase: EDT (+ local thickness unless edt_only, + the reference-order
 // statistics sums when stats).  d_a / d_b are the device inputs for `mode`;
 // results optionally go to d_edt (u32 EDT), d_map (f32 masked diameters) and
-// d_sq (u32 propagated r^2).
+// d_sq (u32 propagated r^2).  xy_done: the x and y passes have already run on
+// this context's buffers (slab by slab, as the inputs arrived), with its
+// counters cleared before them.
 void run_phase(bm_ctx* ctx, Dims dm, const uint8_t* d_a, const uint8_t* d_b, int mode, bool edt_only,
                uint32_t* d_edt, float* d_map, uint32_t* d_sq, float scale, bool stats, cudaStream_t s,
-               PhaseResult& res) {
+               PhaseResult& res, bool xy_done = false) {
   const size_t N = (size_t)dm.n();
   const size_t bits_bytes = (size_t)dm.nw() * dm.h * dm.d * sizeof(uint32_t);
-  uint32_t* A = static_cast<uint32_t*>(ensure(ctx, ctx->dist, N * 4, "distance map"));
-  uint32_t* B = static_cast<uint32_t*>(ensure(ctx, ctx->dist2, N * 4, "distance map"));
-  void* scratch = ensure(ctx, ctx->stack, edt_scratch_bytes(dm), "envelope scratch");
-  uint32_t* selbits = static_cast<uint32_t*>(ensure(ctx, ctx->selbits, bits_bytes, "selection bits"));
-  Counters* ctr = static_cast<Counters*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
-  check(ctx, cudaMemsetAsync(ctr, 0, sizeof(Counters), s), "memset");
-
-  timed(ctx, KF_EDT_X, s, "edt x pass",
-        [&] { return launch_edt_x(d_a, d_b, mode, dm, A, selbits, ctr, s, &ctx->launches); });
-  const size_t redo_bytes = (size_t)dm.w * (dm.h > dm.d ? dm.h : dm.d);
-  uint8_t* redo = static_cast<uint8_t*>(ensure(ctx, ctx->redo, redo_bytes, "line flags"));
-  timed(ctx, KF_EDT_Y, s, "edt y pass",
-        [&] { return launch_edt_window(1, A, B, dm, scratch, redo, ctr, ctx->wait_cycles, s, &ctx->launches); });
+  const EdtBufs eb = edt_buffers(ctx, dm);
+  uint32_t* A = eb.A;
+  uint32_t* B = eb.B;
+  void* scratch = eb.scratch;
+  uint32_t* selbits = eb.selbits;
+  Counters* ctr = eb.ctr;
+  uint8_t* redo = eb.redo;
+  if (!xy_done) {
+    check(ctx, cudaMemsetAsync(ctr, 0, sizeof(Counters), s), "memset");
+    edt_xy(ctx, dm, d_a, d_b, mode, eb, 0, dm.d, s);
+  }
   // local thickness keeps the x pass output (the chain passes read it): the z
   // pass then writes its own map
   uint32_t* E = d_edt ? d_edt
@@ -688,26 +732,45 @@ bm_ctx* twin_of(bm_ctx* ctx) {
   return t;
 }
 
-int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, Dims dm, double spacing,
-                     unsigned flags, bm_stats* th, bm_stats* sp, float* d_thmap, float* d_spmap, cudaStream_t s) {
-  // metrics.rs:70-78
+// metrics.rs:70-78, and the library's flags
+void check_call(bm_ctx* ctx, double spacing, unsigned flags) {
   if (!std::isfinite(spacing) || spacing <= 0.0)
     fail(ctx, BM_ERR_SPACING, "voxel spacings must be finite and positive; got [%g, %g, %g]", spacing, spacing,
          spacing);
   if (flags & ~(unsigned)(BM_FLAG_QUANTILES | BM_FLAG_BONEJ_ROI))
     fail(ctx, BM_ERR_INVALID, "unknown flags 0x%x", flags);
+}
+
+// Work already done by the upload pipeline of bm_tbth_tbsp: the ROI counts, and
+// the x and y passes of either phase.
+struct Prestaged {
+  unsigned long long roi = 0, bone_in_roi = 0;
+  bool bone_xy = false, marrow_xy = false;
+};
+
+bool phases_side_by_side(const bm_ctx* ctx, Dims dm) { return ctx->split_phases && dm.n() <= kSplitMaxVoxels; }
+
+int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, Dims dm, double spacing,
+                     unsigned flags, bm_stats* th, bm_stats* sp, float* d_thmap, float* d_spmap, cudaStream_t s,
+                     const Prestaged* pre = nullptr) {
+  check_call(ctx, spacing, flags);
   const long long N = dm.n();
-  unsigned long long* dcnt =
-      static_cast<unsigned long long*>(ensure(ctx, ctx->counters, sizeof(Counters), "counters"));
-  check(ctx, cudaMemsetAsync(dcnt, 0, 16, s), "memset");
-  timed(ctx, KF_COUNT_ROI, s, "count kernel", [&] {
-    count_roi_kernel<<<152 * 8, 256, 0, s>>>(d_bone, d_roi, N, dcnt);
-    ++ctx->launches;
-    return cudaGetLastError();
-  });
   unsigned long long hc[2];
-  check(ctx, cudaMemcpyAsync(hc, dcnt, 16, cudaMemcpyDeviceToHost, s), "count readback");
-  check(ctx, cudaStreamSynchronize(s), "count kernel");
+  if (pre) {
+    hc[0] = pre->roi;
+    hc[1] = pre->bone_in_roi;
+  } else {
+    unsigned long long* dcnt =
+        static_cast<unsigned long long*>(ensure(ctx, ctx->roicount, 2 * sizeof(unsigned long long), "counts"));
+    check(ctx, cudaMemsetAsync(dcnt, 0, 16, s), "memset");
+    timed(ctx, KF_COUNT_ROI, s, "count kernel", [&] {
+      count_roi_kernel<<<152 * 8, 256, 0, s>>>(d_bone, d_roi, N, dcnt);
+      ++ctx->launches;
+      return cudaGetLastError();
+    });
+    check(ctx, cudaMemcpyAsync(hc, dcnt, 16, cudaMemcpyDeviceToHost, s), "count readback");
+    check(ctx, cudaStreamSynchronize(s), "count kernel");
+  }
   if (hc[0] == 0) fail(ctx, BM_ERR_ROI_EMPTY, "ROI mask contains no included voxels");
   if ((flags & BM_FLAG_BONEJ_ROI) && hc[0] == (unsigned long long)N)
     fail(ctx, BM_ERR_ROI_FULL, "BoneJ compatibility mode requires an ROI mask with both inside and outside voxels");
@@ -727,14 +790,15 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
   // Side by side only while one phase cannot fill the GPU: on 1024^3 the two
   // phases' kernels compete (174 ms against 159 ms one after the other), on
   // 512^3 and below they fill each other's gaps.
-  if (!ctx->split_phases || N > kSplitMaxVoxels) {
+  const bool bone_xy = pre && pre->bone_xy, marrow_xy = pre && pre->marrow_xy;
+  if (!phases_side_by_side(ctx, dm)) {
     float* mb = d_thmap ? d_thmap : qm;
-    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, true, s, rb);
+    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, true, s, rb, bone_xy);
     int st = finish_stats(ctx, rb.acc, rb.osum, th);
     if (st) return st;
     if (want_q && th) quantiles(ctx, mb, N, rb.acc.count, spacing, th, s);
     float* mm = d_spmap ? d_spmap : qm;
-    run_phase(ctx, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, true, s, rm);
+    run_phase(ctx, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, true, s, rm, marrow_xy);
     st = finish_stats(ctx, rm.acc, rm.osum, sp);
     if (st) return st;
     if (want_q && sp) quantiles(ctx, mm, N, rm.acc.count, spacing, sp, s);
@@ -750,7 +814,8 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
     try {
       cudaSetDevice(tw->device);
       check(tw, cudaStreamWaitEvent(tw->stream, ctx->inputs_ready, 0), "stream wait");
-      run_phase(tw, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, true, tw->stream, rm);
+      run_phase(tw, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, false, nullptr, mm, nullptr, scale, true, tw->stream, rm,
+                marrow_xy);
     } catch (const CallError& e) {
       twin_status = e.status;
     } catch (const std::bad_alloc&) {
@@ -760,7 +825,7 @@ int tbth_device_impl(bm_ctx* ctx, const uint8_t* d_bone, const uint8_t* d_roi, D
   });
   int bone_status = BM_OK;
   try {
-    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, true, s, rb);
+    run_phase(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, false, nullptr, mb, nullptr, scale, true, s, rb, bone_xy);
   } catch (const CallError& e) {
     bone_status = e.status;
   }
@@ -785,6 +850,93 @@ uint8_t* stage_input(bm_ctx* ctx, Buffer& b, const uint8_t* host, size_t n, cuda
   uint8_t* d = static_cast<uint8_t*>(ensure(ctx, b, n, "input volume"));
   check(ctx, cudaMemcpyAsync(d, host, n, cudaMemcpyHostToDevice, s), "input upload");
   return d;
+}
+
+// bm_tbth_tbsp from host inputs of at least kPipeMinVoxels: bone and ROI go up
+// on a copy stream in kPipeSlabs slabs of planes, and each slab's ROI counts
+// and x and y passes (of both phases when they run side by side, else of the
+// bone phase) start as soon as the slab has landed, so that the transfer hides
+// most of those passes.  The bails are checked once every slab is counted; the
+// passes that ran before them only wrote the phases' own buffers.
+constexpr long long kPipeMinVoxels = 1ll << 22;
+constexpr int kPipeSlabs = 8;
+
+// On every exit: no copy from the caller's buffers, and no pass reading the
+// uploaded inputs, is left in flight.
+struct UploadFence {
+  bm_ctx* ctx;
+  bm_ctx* twin;
+  ~UploadFence() {
+    if (ctx->upload_stream) cudaStreamSynchronize(ctx->upload_stream);
+    if (twin) cudaStreamSynchronize(twin->stream);
+  }
+};
+
+int tbth_host_pipelined(bm_ctx* ctx, const uint8_t* bone, const uint8_t* roi, Dims dm, double spacing, unsigned flags,
+                        bm_stats* th, bm_stats* sp, float* d_th, float* d_sp, cudaStream_t s) {
+  check_call(ctx, spacing, flags);
+  const size_t N = (size_t)dm.n();
+  uint8_t* d_bone = static_cast<uint8_t*>(ensure(ctx, ctx->in_a, N, "input volume"));
+  uint8_t* d_roi = static_cast<uint8_t*>(ensure(ctx, ctx->in_b, N, "input volume"));
+  if (!ctx->upload_stream)
+    check(ctx, cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking), "stream create");
+  while ((int)ctx->slab_ready.size() < kPipeSlabs) {
+    cudaEvent_t e = nullptr;
+    check(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event create");
+    ctx->slab_ready.push_back(e);
+  }
+  bm_ctx* tw = phases_side_by_side(ctx, dm) ? twin_of(ctx) : nullptr;
+  UploadFence fence{ctx, tw};
+  const EdtBufs eb = edt_buffers(ctx, dm);
+  check(ctx, cudaMemsetAsync(eb.ctr, 0, sizeof(Counters), s), "memset");
+  unsigned long long* dcnt =
+      static_cast<unsigned long long*>(ensure(ctx, ctx->roicount, 2 * sizeof(unsigned long long), "counts"));
+  check(ctx, cudaMemsetAsync(dcnt, 0, 16, s), "memset");
+  // the twin's calls report their errors on this context
+  auto on_twin = [&](auto&& f) {
+    try {
+      f();
+    } catch (const CallError&) {
+      ctx->last_error = tw->last_error;
+      throw;
+    }
+  };
+  EdtBufs et{};
+  if (tw) on_twin([&] {
+    et = edt_buffers(tw, dm);
+    check(tw, cudaMemsetAsync(et.ctr, 0, sizeof(Counters), tw->stream), "memset");
+  });
+  const int K = dm.d < kPipeSlabs ? dm.d : kPipeSlabs;
+  const size_t plane = (size_t)dm.w * dm.h;
+  for (int k = 0; k < K; ++k) {
+    const int z0 = (int)((long long)dm.d * k / K), z1 = (int)((long long)dm.d * (k + 1) / K);
+    const size_t off = (size_t)z0 * plane, len = (size_t)(z1 - z0) * plane;
+    check(ctx, cudaMemcpyAsync(d_bone + off, bone + off, len, cudaMemcpyHostToDevice, ctx->upload_stream),
+          "input upload");
+    check(ctx, cudaMemcpyAsync(d_roi + off, roi + off, len, cudaMemcpyHostToDevice, ctx->upload_stream),
+          "input upload");
+    check(ctx, cudaEventRecord(ctx->slab_ready[k], ctx->upload_stream), "event record");
+    check(ctx, cudaStreamWaitEvent(s, ctx->slab_ready[k], 0), "stream wait");
+    timed(ctx, KF_COUNT_ROI, s, "count kernel", [&] {
+      count_roi_kernel<<<152 * 8, 256, 0, s>>>(d_bone + off, d_roi + off, (long long)len, dcnt);
+      ++ctx->launches;
+      return cudaGetLastError();
+    });
+    edt_xy(ctx, dm, d_bone, d_roi, SEL_BONE_IN_ROI, eb, z0, z1, s);
+    if (tw) on_twin([&] {
+      check(tw, cudaStreamWaitEvent(tw->stream, ctx->slab_ready[k], 0), "stream wait");
+      edt_xy(tw, dm, d_bone, d_roi, SEL_MARROW_IN_ROI, et, z0, z1, tw->stream);
+    });
+  }
+  unsigned long long hc[2];
+  check(ctx, cudaMemcpyAsync(hc, dcnt, 16, cudaMemcpyDeviceToHost, s), "count readback");
+  check(ctx, cudaStreamSynchronize(s), "count kernel");
+  Prestaged pre;
+  pre.roi = hc[0];
+  pre.bone_in_roi = hc[1];
+  pre.bone_xy = true;
+  pre.marrow_xy = tw != nullptr;
+  return tbth_device_impl(ctx, d_bone, d_roi, dm, spacing, flags, th, sp, d_th, d_sp, s, &pre);
 }
 
 }  // namespace
@@ -868,8 +1020,13 @@ void bm_ctx_destroy(bm_ctx* ctx) {
     if (ctx->twin) bm_ctx_destroy(ctx->twin);
     ctx->twin = nullptr;
     if (ctx->inputs_ready) cudaEventDestroy(ctx->inputs_ready);
+    if (ctx->upload_stream) {
+      cudaStreamSynchronize(ctx->upload_stream);
+      cudaStreamDestroy(ctx->upload_stream);
+    }
+    for (cudaEvent_t e : ctx->slab_ready) cudaEventDestroy(e);
     for (Buffer* b : work_buffers(ctx)) release(*b);
-    for (Buffer* b : {&ctx->lut, &ctx->counters, &ctx->host_pinned, &ctx->fillinfo}) release(*b);
+    for (Buffer* b : {&ctx->lut, &ctx->counters, &ctx->roicount, &ctx->host_pinned, &ctx->fillinfo}) release(*b);
     for (const ProfRec& r : ctx->prof) {
       cudaEventDestroy(r.start);
       cudaEventDestroy(r.stop);
@@ -1130,11 +1287,16 @@ int bm_tbth_tbsp(bm_ctx* ctx, const uint8_t* bone, const uint8_t* roi, size_t wi
     const Dims dm = check_dims(ctx, width, height, depth);
     const size_t N = (size_t)dm.n();
     cudaStream_t s = ctx->stream;
-    const uint8_t* d_bone = stage_input(ctx, ctx->in_a, bone, N, s);
-    const uint8_t* d_roi = stage_input(ctx, ctx->in_b, roi, N, s);
     float* d_th = thickness_map ? static_cast<float*>(ensure(ctx, ctx->outmap, N * 4, "output")) : nullptr;
     float* d_sp = spacing_map ? static_cast<float*>(ensure(ctx, ctx->outmap2, N * 4, "output")) : nullptr;
-    int st = tbth_device_impl(ctx, d_bone, d_roi, dm, spacing_um, flags, thickness, spacing, d_th, d_sp, s);
+    int st;
+    if ((long long)N >= kPipeMinVoxels) {
+      st = tbth_host_pipelined(ctx, bone, roi, dm, spacing_um, flags, thickness, spacing, d_th, d_sp, s);
+    } else {
+      const uint8_t* d_bone = stage_input(ctx, ctx->in_a, bone, N, s);
+      const uint8_t* d_roi = stage_input(ctx, ctx->in_b, roi, N, s);
+      st = tbth_device_impl(ctx, d_bone, d_roi, dm, spacing_um, flags, thickness, spacing, d_th, d_sp, s);
+    }
     if (st) return st;
     if (thickness_map)
       check(ctx, cudaMemcpyAsync(thickness_map, d_th, N * 4, cudaMemcpyDeviceToHost, s), "result download");

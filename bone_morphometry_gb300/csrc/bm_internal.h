@@ -209,6 +209,7 @@ struct bm_ctx {
   bm::Buffer selbits, ridgebits; // row-padded bitmasks: selected voxels, ridge voxels
   bm::Buffer ridges;           // ridge records
   bm::Buffer counters;         // bm::Counters
+  bm::Buffer roicount;         // ROI and bone-in-ROI voxel counts (the bails of bm_tbth_tbsp)
   bm::Buffer accum;            // bm::StatsAccum
   bm::Buffer cpart;            // bm::FixedPartial per cleanup CTA
   bm::Buffer outmap;           // f32 output staging
@@ -227,6 +228,11 @@ struct bm_ctx {
   uint32_t surf_max = 0;
 
   // profiler: CUDA events around every library launch while enabled
+  // bm_tbth_tbsp's upload pipeline: a copy stream and one event per slab of
+  // planes (created on first use)
+  cudaStream_t upload_stream = nullptr;
+  std::vector<cudaEvent_t> slab_ready;
+
   bool profiling = false;
   std::vector<bm::ProfRec> prof;
   std::vector<cudaEvent_t> event_pool;
