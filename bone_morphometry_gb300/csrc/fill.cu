@@ -386,10 +386,10 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
           }
           const uint32_t se = min(min(e, s_whi), ss + (uint32_t)kRound);
           const uint32_t wb = ss - s_wlo;  // window index of the round's first ball
-          // test: four balls per warp step, two per half-warp (lanes 0..15 on
-          // balls 4w and 4w+2, lanes 16..31 on 4w+1 and 4w+3); lane hl tests
-          // plane zlo + hl of each.  Written without branches so that the two
-          // balls' tests interleave.
+          // test: two balls per warp step, one per half-warp (lanes 0..15 on
+          // ball 2w, lanes 16..31 on 2w+1); lane hl tests plane zlo + hl of its
+          // ball.  Two balls per step spread a round's balls over all warps
+          // (four per step measured 2% slower: the last steps left warps idle).
           auto plane_test = [&](uint32_t bi, int& pya, int& pyb, int& zz) -> bool {
             const bool have = bi < se - ss;
             const uint32_t c = ent[wb + (have ? bi : 0u)];
@@ -422,13 +422,11 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
                     ((wb + bi) << 16) | ((uint32_t)(pyb - pya) << 10) | ((uint32_t)pya << 4) | (uint32_t)zz;
             }
           };
-          for (uint32_t bp = 4 * warp; bp < se - ss; bp += 4 * kFillWarps) {
-            const uint32_t b1 = bp + half, b2 = bp + 2 + half;
-            int ya1, yb1, z1, ya2, yb2, z2;
+          for (uint32_t bp = 2 * warp; bp < se - ss; bp += 2 * kFillWarps) {
+            const uint32_t b1 = bp + half;
+            int ya1, yb1, z1;
             const bool p1 = plane_test(b1, ya1, yb1, z1);
-            const bool p2 = plane_test(b2, ya2, yb2, z2);
             append(b1, p1, ya1, yb1, z1);
-            append(b2, p2, ya2, yb2, z2);
           }
           __syncthreads();
           // paint: G threads per item (G = 1 .. 8, about twice as many as keep
