@@ -74,9 +74,17 @@ void copy_message(bm_result& r, const char* msg) {
 
 }  // namespace
 
+// Settings every worker context takes from the pool (no effect on results).
+struct PoolSettings {
+  int site_method = BM_SITES_AUTO;
+  bool split_phases = true;
+  bool operator==(const PoolSettings& o) const { return site_method == o.site_method && split_phases == o.split_phases; }
+};
+
 class Pool {
  public:
-  Pool(int device, int workers, double budget) : device_(device), budget_(budget) {
+  Pool(int device, int workers, double budget, PoolSettings settings)
+      : device_(device), budget_(budget), settings_(settings) {
     for (int i = 0; i < workers; ++i) {
       bm_ctx* c = nullptr;
       const int st = bm_ctx_create(device, &c);
@@ -84,6 +92,8 @@ class Pool {
         status_ = st;
         break;
       }
+      c->site_method = settings.site_method;
+      c->split_phases = settings.split_phases;
       ctxs_.push_back(c);
     }
     if (status_ == BM_OK)
@@ -102,6 +112,7 @@ class Pool {
 
   int status() const { return status_; }
   double budget() const { return budget_; }
+  const PoolSettings& settings() const { return settings_; }
 
   void submit(Job* j) {
     {
@@ -244,6 +255,7 @@ class Pool {
 
   int device_;
   double budget_;
+  PoolSettings settings_;
   int status_ = BM_OK;
   std::vector<bm_ctx*> ctxs_;
   std::vector<std::thread> threads_;
@@ -255,8 +267,8 @@ class Pool {
   bool stop_ = false;
 };
 
-Pool* pool_create(int device, int workers, double budget, int* status) {
-  Pool* p = new Pool(device, workers, budget);
+Pool* pool_create(int device, int workers, double budget, PoolSettings settings, int* status) {
+  Pool* p = new Pool(device, workers, budget, settings);
   if (p->status() != BM_OK) {
     *status = p->status();
     delete p;
@@ -306,9 +318,17 @@ int bm_batch_tbth_tbsp(bm_ctx* ctx, const bm_specimen* items, size_t n, int devi
                        bm_stats* thickness, bm_stats* spacing, int* status) {
   if (!ctx || (n && !items)) return BM_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->pool_mu);
+  // the workers take the context's site method and phase scheduling
+  PoolSettings want;
+  want.site_method = ctx->site_method;
+  want.split_phases = ctx->split_phases;
+  if (ctx->pool && !(ctx->pool->settings() == want)) {
+    pool_destroy(ctx->pool);
+    ctx->pool = nullptr;
+  }
   if (!ctx->pool) {
     int st = BM_OK;
-    ctx->pool = pool_create(ctx->device, ctx->workers, 1e300, &st);
+    ctx->pool = pool_create(ctx->device, ctx->workers, 1e300, want, &st);
     if (!ctx->pool) return st;
   }
   std::vector<Job> jobs(n);
@@ -342,7 +362,7 @@ int bm_server_create(int device, int workers, double hbm_budget_bytes, bm_server
   if (!out || workers < 1 || workers > 64 || !(hbm_budget_bytes > 0)) return BM_ERR_INVALID;
   *out = nullptr;
   int st = BM_OK;
-  Pool* p = pool_create(device, workers, hbm_budget_bytes, &st);
+  Pool* p = pool_create(device, workers, hbm_budget_bytes, PoolSettings{}, &st);
   if (!p) return st;
   bm_server* s = new bm_server();
   s->pool.reset(p);

@@ -13,13 +13,17 @@ per-specimen arithmetic, so every result equals the specimen's result alone.
 from __future__ import annotations
 
 import ctypes
+import json
+import math
 import os
+import tempfile
+import time
 from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import (BM_ERR_BUSY, BM_OK, BmResult, BmSpecimen, BmStats, BoneMorphometryError, Context, default_context,
-                   last_error, load, raise_for)
+from ._lib import (BM_ERR_BUSY, BM_OK, BM_SITES_AUTO, BM_SITES_CHAINS, BM_SITES_SPHERES, BmResult, BmSpecimen,
+                   BmStats, BoneMorphometryError, Context, default_context, last_error, load, raise_for)
 from .api import DistributionStats, FeatureMode, _flags, _is_cuda_tensor
 
 
@@ -65,6 +69,119 @@ def batch_tbth_tbsp(specimens, feature_mode=FeatureMode.CLASSIC, ctx: Context | 
     st = (ctypes.c_int * len(items))()
     lib.bm_batch_tbth_tbsp(ctx.handle, arr, len(items), 1 if device else 0, _flags(feature_mode), th, spc, st)
     return [(DistributionStats.from_c(th[i]), DistributionStats.from_c(spc[i]), int(st[i])) for i in range(len(items))]
+
+
+# ---- settings of the batched form, picked by measurement ----------------------------------
+#
+# Three settings change how fast a batch runs and never what it returns: the
+# number of workers, how the fill finds the non-selected voxels that ridge
+# spheres reach (the sphere lattice points, a scatter per ridge, or the chain
+# passes, a gather along the distance transform's argmins; local_thickness.rs:169-202
+# paints them too), and whether each specimen's two phases run side by side.
+# The tuner runs the whole batch once per candidate and keeps the fastest,
+# per GPU and per mix of specimen sizes, in a JSON file, so a later batch of the
+# same kind starts from the stored choice.
+
+TUNE_CANDIDATES = tuple((w, m, c) for w in (2, 4, 6, 8) for m in (BM_SITES_AUTO, BM_SITES_SPHERES, BM_SITES_CHAINS)
+                        for c in (True, False))
+
+
+@dataclass
+class Tuning:
+    workers: int
+    site_method: int
+    concurrent_phases: bool
+    batch_ms: float          # the chosen candidate's time when it was measured
+    from_cache: bool = False
+
+
+def tuning_cache_path() -> str:
+    """BM_TUNE_CACHE, else ~/.cache/bone_morphometry_gb300/batch_tuning.json."""
+    return os.environ.get("BM_TUNE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache",
+                                                           "bone_morphometry_gb300", "batch_tuning.json")
+
+
+def mix_signature(shapes) -> str:
+    """Buckets of a mix: specimen count (octaves), total and largest voxel
+    counts (half octaves)."""
+    vox = [int(np.prod(s)) for s in shapes]
+    if not vox:
+        return "empty"
+    half_octave = lambda v: int(round(2.0 * math.log2(max(v, 1))))
+    return "n%d-t%d-m%d" % (len(vox).bit_length(), half_octave(sum(vox)), half_octave(max(vox)))
+
+
+def device_key(device: int = 0) -> str:
+    try:
+        import torch
+
+        return torch.cuda.get_device_name(device)
+    except Exception:
+        return "cuda:%d" % device
+
+
+def _load_cache(path: str) -> dict:
+    try:
+        with open(path) as f:
+            data = json.load(f)
+        return data if isinstance(data, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def _save_cache(path: str, data: dict) -> None:
+    d = os.path.dirname(path) or "."
+    os.makedirs(d, exist_ok=True)
+    fd, tmp = tempfile.mkstemp(dir=d, prefix=".tuning-", suffix=".json")
+    with os.fdopen(fd, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)  # readers see the old file or the new one, never a partial one
+
+
+def autotune(run, key: str, path: str, candidates=TUNE_CANDIDATES, retune: bool = False,
+             clock=time.perf_counter):
+    """run(workers, site_method, concurrent_phases) -> results.  On a cache
+    miss (or retune) every candidate runs once after one untimed warm-up run
+    and the fastest is stored under key; on a hit only the stored candidate
+    runs.  Returns (results, Tuning)."""
+    cache = _load_cache(path)
+    hit = cache.get(key)
+    if hit is not None and not retune:
+        t = Tuning(int(hit["workers"]), int(hit["site_method"]), bool(hit["concurrent_phases"]),
+                   float(hit["batch_ms"]), True)
+        return run(t.workers, t.site_method, t.concurrent_phases), t
+    cands = list(candidates)
+    run(*cands[0])  # warm-up: device buffers grown, tables built
+    best = None
+    for cand in cands:
+        t0 = clock()
+        res = run(*cand)
+        dt = clock() - t0
+        if best is None or dt < best[0]:
+            best = (dt, cand, res)
+    dt, (w, m, c), res = best
+    t = Tuning(int(w), int(m), bool(c), 1e3 * dt)
+    cache[key] = {"workers": t.workers, "site_method": t.site_method, "concurrent_phases": t.concurrent_phases,
+                  "batch_ms": round(t.batch_ms, 3)}
+    _save_cache(path, cache)
+    return res, t
+
+
+def tuned_batch_tbth_tbsp(specimens, feature_mode=FeatureMode.CLASSIC, ctx: Context | None = None,
+                          cache_path: str | None = None, retune: bool = False, candidates=TUNE_CANDIDATES):
+    """batch_tbth_tbsp with the settings the tuner picks for this GPU and mix
+    (they stay set on the context).  Returns ([(thickness, spacing, status)], Tuning)."""
+    ctx = ctx or default_context()
+    items = list(specimens)
+    key = device_key(ctx.device) + "|" + mix_signature([tuple(sp.bone.shape) for sp in items])
+
+    def run(workers, site_method, concurrent):
+        ctx.call("bm_ctx_set_workers", int(workers))
+        ctx.set_site_method(site_method)
+        ctx.set_concurrent_phases(concurrent)
+        return batch_tbth_tbsp(items, feature_mode, ctx)
+
+    return autotune(run, key, cache_path or tuning_cache_path(), candidates, retune)
 
 
 def footprint_bytes(shape) -> int:

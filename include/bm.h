@@ -207,10 +207,12 @@ typedef struct bm_specimen {
 /* Tb.Th / Tb.Sp of n specimens of uneven sizes.  The context's worker pool
  * (bm_ctx_set_workers; by default 4 workers, each with its own stream and
  * buffers) takes specimens as workers free up, so their kernels overlap on the
- * GPU.  Per-specimen results and statuses go to thickness[i], spacing[i],
- * status[i]; the call returns BM_OK when every specimen succeeded, else the
- * first non-zero status (the others still complete).  device_pointers != 0:
- * bone/roi are device pointers on the context's device. */
+ * GPU.  The workers take the context's site method and phase scheduling
+ * (bm_ctx_set_site_method, bm_ctx_set_concurrent_phases; the pool is recreated
+ * when they change).  Per-specimen results and statuses go to thickness[i],
+ * spacing[i], status[i]; the call returns BM_OK when every specimen succeeded,
+ * else the first non-zero status (the others still complete).
+ * device_pointers != 0: bone/roi are device pointers on the context's device. */
 int bm_batch_tbth_tbsp(bm_ctx* ctx, const bm_specimen* items, size_t n, int device_pointers, unsigned flags,
                        bm_stats* thickness, bm_stats* spacing, int* status);
 /* Set the number of workers of the context's pool (1..64; recreates the pool). */

@@ -1,0 +1,83 @@
+"""The batched form's tuner (serving.autotune): candidates timed once each after
+a warm-up, the fastest stored per key in a JSON cache, a cache hit running only
+the stored candidate.  Host logic only (a fake batch and clock)."""
+
+import json
+
+from bone_morphometry_gb300 import serving as SV
+from bone_morphometry_gb300._lib import BM_SITES_AUTO, BM_SITES_CHAINS, BM_SITES_SPHERES
+
+
+class FakeBatch:
+    """Pretends each candidate takes cost[(w, m, c)] seconds on a fake clock."""
+
+    def __init__(self, cost):
+        self.cost = cost
+        self.now = 0.0
+        self.calls = []
+
+    def clock(self):
+        return self.now
+
+    def run(self, w, m, c):
+        self.calls.append((w, m, c))
+        self.now += self.cost[(w, m, c)]
+        return ["result"]
+
+
+CANDS = ((2, BM_SITES_AUTO, True), (4, BM_SITES_SPHERES, False), (8, BM_SITES_CHAINS, True))
+
+
+def test_picks_the_fastest_and_persists(tmp_path):
+    path = str(tmp_path / "sub" / "tuning.json")
+    fb = FakeBatch({CANDS[0]: 0.30, CANDS[1]: 0.10, CANDS[2]: 0.20})
+    res, t = SV.autotune(fb.run, "gpu|mix", path, CANDS, clock=fb.clock)
+    assert res == ["result"]
+    assert (t.workers, t.site_method, t.concurrent_phases) == (4, BM_SITES_SPHERES, False)
+    assert abs(t.batch_ms - 100.0) < 1e-9 and not t.from_cache
+    assert fb.calls == [CANDS[0]] + list(CANDS)  # one warm-up, then each candidate once
+    stored = json.load(open(path))
+    assert stored == {"gpu|mix": {"workers": 4, "site_method": BM_SITES_SPHERES, "concurrent_phases": False,
+                                  "batch_ms": 100.0}}
+
+
+def test_cache_hit_runs_only_the_stored_candidate(tmp_path):
+    path = str(tmp_path / "tuning.json")
+    fb = FakeBatch({CANDS[0]: 0.3, CANDS[1]: 0.2, CANDS[2]: 0.1})
+    SV.autotune(fb.run, "k", path, CANDS, clock=fb.clock)
+    fb.calls.clear()
+    res, t = SV.autotune(fb.run, "k", path, CANDS, clock=fb.clock)
+    assert t.from_cache and (t.workers, t.site_method, t.concurrent_phases) == CANDS[2]
+    assert fb.calls == [CANDS[2]] and res == ["result"]
+    # another key tunes again and keeps the first entry
+    fb.calls.clear()
+    SV.autotune(fb.run, "k2", path, CANDS, clock=fb.clock)
+    assert len(fb.calls) == 4 and set(json.load(open(path))) == {"k", "k2"}
+
+
+def test_retune_and_unreadable_cache(tmp_path):
+    path = tmp_path / "tuning.json"
+    path.write_text("{not json")
+    fb = FakeBatch({CANDS[0]: 0.1, CANDS[1]: 0.2, CANDS[2]: 0.3})
+    _, t = SV.autotune(fb.run, "k", str(path), CANDS, clock=fb.clock)
+    assert (t.workers, t.from_cache) == (2, False)
+    fb.cost[CANDS[0]] = 0.5
+    _, t = SV.autotune(fb.run, "k", str(path), CANDS, retune=True, clock=fb.clock)
+    assert (t.workers, t.site_method) == (4, BM_SITES_SPHERES)
+    assert json.load(open(path))["k"]["workers"] == 4
+
+
+def test_mix_signature_buckets():
+    a = SV.mix_signature([(96, 100, 120), (384, 300, 200)])
+    b = SV.mix_signature([(200, 300, 384), (120, 100, 96)])  # order and axis order do not matter
+    assert a == b
+    assert SV.mix_signature([(128, 128, 128)] * 64) != SV.mix_signature([(128, 128, 128)] * 8)
+    assert SV.mix_signature([(128, 128, 128)]) != SV.mix_signature([(256, 256, 256)])
+    assert SV.mix_signature([]) == "empty"
+
+
+def test_default_cache_path(monkeypatch, tmp_path):
+    monkeypatch.setenv("BM_TUNE_CACHE", str(tmp_path / "x.json"))
+    assert SV.tuning_cache_path() == str(tmp_path / "x.json")
+    monkeypatch.delenv("BM_TUNE_CACHE")
+    assert SV.tuning_cache_path().endswith("batch_tuning.json")
