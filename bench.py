@@ -306,9 +306,12 @@ def bench_batch(ctx, n_items=64):
         return out
 
     plain()  # warm buffers
-    t0 = time.perf_counter()
-    ref = plain()
-    t_plain = time.perf_counter() - t0
+    plain_times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        ref = plain()
+        plain_times.append(time.perf_counter() - t0)
+    t_plain = min(plain_times)
     # device time of the plain loop's kernels, each with the GPU to itself (phases one
     # after the other, so that no two timed kernels overlap)
     ctx.set_concurrent_phases(False)
@@ -318,12 +321,13 @@ def bench_batch(ctx, n_items=64):
     ctx.profile(False)
     ctx.set_concurrent_phases(True)
     t0 = time.perf_counter()
-    _, tuning = tuned_batch_tbth_tbsp(dev, ctx=ctx)  # on a cache miss: every candidate once
+    _, tuning = tuned_batch_tbth_tbsp(dev, ctx=ctx)  # on a cache miss: every candidate, warm-up + 2 runs
     tune_s = time.perf_counter() - t0
+    tuned_batch_tbth_tbsp(dev, ctx=ctx)  # the stored choice: its pool's buffers grown
     times = []
-    for _ in range(2):
+    for _ in range(3):
         t0 = time.perf_counter()
-        res, _ = tuned_batch_tbth_tbsp(dev, ctx=ctx)  # the stored choice
+        res, _ = tuned_batch_tbth_tbsp(dev, ctx=ctx)
         times.append(time.perf_counter() - t0)
     t_batch = min(times)
     ctx.set_site_method(0)
@@ -332,7 +336,9 @@ def bench_batch(ctx, n_items=64):
                and r[0].standard_deviation == a.thickness.standard_deviation for r, a in zip(res, ref))
     return {"specimens": n_items, "voxels": vox, "plain_gvoxel_s": vox / t_plain / 1e9,
             "batched_gvoxel_s": vox / t_batch / 1e9, "speedup": t_plain / t_batch, "plain_ms": 1e3 * t_plain,
-            "batched_ms": 1e3 * t_batch, "workers": tuning.workers,
+            "batched_ms": 1e3 * t_batch, "workers": tuning.workers, "timing": "best of 3 runs of each form",
+            "plain_ms_runs": [round(1e3 * t, 2) for t in plain_times],
+            "batched_ms_runs": [round(1e3 * t, 2) for t in times],
             "kernels_one_at_a_time_ms": round(busy_ms, 2),
             "kernels_one_at_a_time_gvoxel_s": vox / (busy_ms * 1e-3) / 1e9,
             "tuning": {"workers": tuning.workers, "site_method": ["auto", "spheres", "chains"][tuning.site_method],

@@ -306,6 +306,7 @@ uint64_t bm_footprint_bytes(size_t width, size_t height, size_t depth) {
 int bm_ctx_set_workers(bm_ctx* ctx, int workers) {
   if (!ctx || workers < 1 || workers > 64) return BM_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->pool_mu);
+  if (workers == ctx->workers) return BM_OK;  // the pool stays (with its grown buffers)
   if (ctx->pool) {
     pool_destroy(ctx->pool);
     ctx->pool = nullptr;

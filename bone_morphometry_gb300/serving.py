@@ -139,26 +139,28 @@ def _save_cache(path: str, data: dict) -> None:
 
 
 def autotune(run, key: str, path: str, candidates=TUNE_CANDIDATES, retune: bool = False,
-             clock=time.perf_counter):
+             clock=time.perf_counter, repeats: int = 2):
     """run(workers, site_method, concurrent_phases) -> results.  On a cache
-    miss (or retune) every candidate runs once after one untimed warm-up run
-    and the fastest is stored under key; on a hit only the stored candidate
-    runs.  Returns (results, Tuning)."""
+    miss (or retune) every candidate runs once untimed (a new setting gives
+    the pool new worker contexts, whose buffers grow on their first batch),
+    then `repeats` times timed; the candidate with the fastest run is stored
+    under key.  On a hit only the stored candidate runs.  Returns (results,
+    Tuning)."""
     cache = _load_cache(path)
     hit = cache.get(key)
     if hit is not None and not retune:
         t = Tuning(int(hit["workers"]), int(hit["site_method"]), bool(hit["concurrent_phases"]),
                    float(hit["batch_ms"]), True)
         return run(t.workers, t.site_method, t.concurrent_phases), t
-    cands = list(candidates)
-    run(*cands[0])  # warm-up: device buffers grown, tables built
     best = None
-    for cand in cands:
-        t0 = clock()
-        res = run(*cand)
-        dt = clock() - t0
-        if best is None or dt < best[0]:
-            best = (dt, cand, res)
+    for cand in candidates:
+        run(*cand)  # warm-up of this setting
+        for _ in range(max(1, repeats)):
+            t0 = clock()
+            res = run(*cand)
+            dt = clock() - t0
+            if best is None or dt < best[0]:
+                best = (dt, cand, res)
     dt, (w, m, c), res = best
     t = Tuning(int(w), int(m), bool(c), 1e3 * dt)
     cache[key] = {"workers": t.workers, "site_method": t.site_method, "concurrent_phases": t.concurrent_phases,

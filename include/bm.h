@@ -215,7 +215,8 @@ typedef struct bm_specimen {
  * device_pointers != 0: bone/roi are device pointers on the context's device. */
 int bm_batch_tbth_tbsp(bm_ctx* ctx, const bm_specimen* items, size_t n, int device_pointers, unsigned flags,
                        bm_stats* thickness, bm_stats* spacing, int* status);
-/* Set the number of workers of the context's pool (1..64; recreates the pool). */
+/* Set the number of workers of the context's pool (1..64; recreates the pool
+ * when the count changes). */
 int bm_ctx_set_workers(bm_ctx* ctx, int workers);
 
 /* Request server: submitted specimens (host pointers) are admitted in arrival

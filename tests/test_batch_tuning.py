@@ -1,5 +1,5 @@
-"""The batched form's tuner (serving.autotune): candidates timed once each after
-a warm-up, the fastest stored per key in a JSON cache, a cache hit running only
+"""The batched form's tuner (serving.autotune): each candidate timed after its own
+warm-up, the fastest stored per key in a JSON cache, a cache hit running only
 the stored candidate.  Host logic only (a fake batch and clock)."""
 
 import json
@@ -35,7 +35,7 @@ def test_picks_the_fastest_and_persists(tmp_path):
     assert res == ["result"]
     assert (t.workers, t.site_method, t.concurrent_phases) == (4, BM_SITES_SPHERES, False)
     assert abs(t.batch_ms - 100.0) < 1e-9 and not t.from_cache
-    assert fb.calls == [CANDS[0]] + list(CANDS)  # one warm-up, then each candidate once
+    assert fb.calls == [c for c in CANDS for _ in range(3)]  # each candidate: a warm-up, then two timed runs
     stored = json.load(open(path))
     assert stored == {"gpu|mix": {"workers": 4, "site_method": BM_SITES_SPHERES, "concurrent_phases": False,
                                   "batch_ms": 100.0}}
@@ -52,7 +52,7 @@ def test_cache_hit_runs_only_the_stored_candidate(tmp_path):
     # another key tunes again and keeps the first entry
     fb.calls.clear()
     SV.autotune(fb.run, "k2", path, CANDS, clock=fb.clock)
-    assert len(fb.calls) == 4 and set(json.load(open(path))) == {"k", "k2"}
+    assert len(fb.calls) == 9 and set(json.load(open(path))) == {"k", "k2"}
 
 
 def test_retune_and_unreadable_cache(tmp_path):
