@@ -82,7 +82,7 @@ def batch_tbth_tbsp(specimens, feature_mode=FeatureMode.CLASSIC, ctx: Context | 
 # per GPU and per mix of specimen sizes, in a JSON file, so a later batch of the
 # same kind starts from the stored choice.
 
-TUNE_CANDIDATES = tuple((w, m, c) for w in (2, 4, 6, 8) for m in (BM_SITES_AUTO, BM_SITES_SPHERES, BM_SITES_CHAINS)
+TUNE_CANDIDATES = tuple((w, m, c) for w in (2, 4, 6, 8, 12) for m in (BM_SITES_AUTO, BM_SITES_SPHERES, BM_SITES_CHAINS)
                         for c in (True, False))
 
 
