@@ -139,13 +139,13 @@ def _save_cache(path: str, data: dict) -> None:
 
 
 def autotune(run, key: str, path: str, candidates=TUNE_CANDIDATES, retune: bool = False,
-             clock=time.perf_counter, repeats: int = 2):
+             clock=time.perf_counter, repeats: int = 3):
     """run(workers, site_method, concurrent_phases) -> results.  On a cache
     miss (or retune) every candidate runs once untimed (a new setting gives
     the pool new worker contexts, whose buffers grow on their first batch),
-    then `repeats` times timed; the candidate with the fastest run is stored
-    under key.  On a hit only the stored candidate runs.  Returns (results,
-    Tuning)."""
+    then `repeats` times timed; the candidate with the lowest median time is
+    stored under key (single batch times vary by ~15% from run to run).  On a
+    hit only the stored candidate runs.  Returns (results, Tuning)."""
     cache = _load_cache(path)
     hit = cache.get(key)
     if hit is not None and not retune:
@@ -155,12 +155,14 @@ def autotune(run, key: str, path: str, candidates=TUNE_CANDIDATES, retune: bool 
     best = None
     for cand in candidates:
         run(*cand)  # warm-up of this setting
+        times = []
         for _ in range(max(1, repeats)):
             t0 = clock()
             res = run(*cand)
-            dt = clock() - t0
-            if best is None or dt < best[0]:
-                best = (dt, cand, res)
+            times.append(clock() - t0)
+        dt = sorted(times)[len(times) // 2]
+        if best is None or dt < best[0]:
+            best = (dt, cand, res)
     dt, (w, m, c), res = best
     t = Tuning(int(w), int(m), bool(c), 1e3 * dt)
     cache[key] = {"workers": t.workers, "site_method": t.site_method, "concurrent_phases": t.concurrent_phases,

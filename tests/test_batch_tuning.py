@@ -1,6 +1,6 @@
 """The batched form's tuner (serving.autotune): each candidate timed after its own
-warm-up, the fastest stored per key in a JSON cache, a cache hit running only
-the stored candidate.  Host logic only (a fake batch and clock)."""
+warm-up, the one with the lowest median stored per key in a JSON cache, a cache
+hit running only the stored candidate.  Host logic only (a fake batch and clock)."""
 
 import json
 
@@ -35,7 +35,7 @@ def test_picks_the_fastest_and_persists(tmp_path):
     assert res == ["result"]
     assert (t.workers, t.site_method, t.concurrent_phases) == (4, BM_SITES_SPHERES, False)
     assert abs(t.batch_ms - 100.0) < 1e-9 and not t.from_cache
-    assert fb.calls == [c for c in CANDS for _ in range(3)]  # each candidate: a warm-up, then two timed runs
+    assert fb.calls == [c for c in CANDS for _ in range(4)]  # each candidate: a warm-up, then three timed runs
     stored = json.load(open(path))
     assert stored == {"gpu|mix": {"workers": 4, "site_method": BM_SITES_SPHERES, "concurrent_phases": False,
                                   "batch_ms": 100.0}}
@@ -52,7 +52,22 @@ def test_cache_hit_runs_only_the_stored_candidate(tmp_path):
     # another key tunes again and keeps the first entry
     fb.calls.clear()
     SV.autotune(fb.run, "k2", path, CANDS, clock=fb.clock)
-    assert len(fb.calls) == 9 and set(json.load(open(path))) == {"k", "k2"}
+    assert len(fb.calls) == 12 and set(json.load(open(path))) == {"k", "k2"}
+
+
+def test_median_not_a_lucky_run(tmp_path):
+    """A candidate with one fast outlier loses to one that is steadily faster."""
+    seq = {CANDS[0]: [0.5, 0.05, 0.5, 0.5], CANDS[1]: [0.2, 0.2, 0.2, 0.2], CANDS[2]: [0.3, 0.3, 0.3, 0.3]}
+
+    class Seq(FakeBatch):
+        def run(self, w, m, c):
+            self.calls.append((w, m, c))
+            self.now += seq[(w, m, c)].pop(0)
+            return ["r"]
+
+    fb = Seq({})
+    _, t = SV.autotune(fb.run, "k", str(tmp_path / "t.json"), CANDS, clock=fb.clock)
+    assert (t.workers, t.site_method) == (4, BM_SITES_SPHERES)
 
 
 def test_retune_and_unreadable_cache(tmp_path):
