@@ -603,7 +603,18 @@ def run_gpu(args, rank, world, local):
 
     kernels, roofline, edt_roof = kernel_report(m["ktimes"], n_vox, committed_traffic().get(args.workload, {}))
 
-    # -- CPU baseline (rank 0, N = 1 only): the oracle on a bounded sample --------------------
+    extras = {}
+    if world == 1 and not args.no_extras:
+        if args.workload != "single1024":
+            extras["single1024"] = bench_single1024(args, local)
+        extras["batch64"] = bench_batch(ctx)
+        extras["serving"] = bench_serving(args.serve_requests, args.serve_rate)
+        if args.serve_rate_light > 0:
+            # the same mix at a rate the GPU keeps up with: latency without a growing queue
+            extras["serving_light"] = bench_serving(args.serve_requests, args.serve_rate_light)
+
+    # -- CPU baseline (rank 0, N = 1 only): the oracle on a bounded sample, after every GPU leg
+    # (its host threads then cannot slow the GPU legs' host side) --------------------------------
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -618,16 +629,6 @@ def run_gpu(args, rank, world, local):
                "sample": "z-slab %dx%dx%d of the same specimen, both phases, %.1f s" % (w, h, slices, dt),
                "value_1_thread": vox1 / dt1 / 1e9,
                "sample_1_thread": "z-slab %dx%dx%d, both phases, %.1f s" % (w, h, slices1, dt1)}
-
-    extras = {}
-    if world == 1 and not args.no_extras:
-        if args.workload != "single1024":
-            extras["single1024"] = bench_single1024(args, local)
-        extras["batch64"] = bench_batch(ctx)
-        extras["serving"] = bench_serving(args.serve_requests, args.serve_rate)
-        if args.serve_rate_light > 0:
-            # the same mix at a rate the GPU keeps up with: latency without a growing queue
-            extras["serving_light"] = bench_serving(args.serve_requests, args.serve_rate_light)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
