@@ -332,6 +332,7 @@ def bench_batch(ctx, n_items=64):
         times.append(time.perf_counter() - t0)
     t_batch = min(times)
     ctx.set_site_method(0)
+    ctx.set_fill_tile_rows(0)
     ctx.set_concurrent_phases(True)
     same = all(r[2] == 0 and r[0].mean == a.thickness.mean and r[1].mean == a.spacing.mean
                and r[0].standard_deviation == a.thickness.standard_deviation for r, a in zip(res, ref))
@@ -343,6 +344,7 @@ def bench_batch(ctx, n_items=64):
             "kernels_one_at_a_time_ms": round(busy_ms, 2),
             "kernels_one_at_a_time_gvoxel_s": vox / (busy_ms * 1e-3) / 1e9,
             "tuning": {"workers": tuning.workers, "site_method": ["auto", "spheres", "chains"][tuning.site_method],
+                       "fill_tile_rows": tuning.fill_tile_rows,
                        "concurrent_phases": tuning.concurrent_phases, "candidates": len(TUNE_CANDIDATES),
                        "from_cache": tuning.from_cache, "tuned_batch_ms": round(tuning.batch_ms, 2),
                        "tuning_s": round(tune_s, 2)},

@@ -135,6 +135,7 @@ SIGNATURES = {
     "bm_footprint_bytes": (ctypes.c_uint64, [_sz, _sz, _sz]),
     "bm_ctx_set_concurrent_phases": (_i, [_vp, _i]),
     "bm_ctx_set_site_method": (_i, [_vp, _i]),
+    "bm_ctx_set_fill_tile_rows": (_i, [_vp, _i]),
     "bm_ctx_set_wait_cycles": (_i, [_vp, ctypes.c_longlong]),
     "bm_tiff_read": (_i, [ctypes.c_char_p, ctypes.c_uint, _i, _vp, _sz, ctypes.POINTER(_sz), ctypes.POINTER(_sz),
                           ctypes.POINTER(_sz)]),
@@ -223,6 +224,10 @@ class Context:
         """How the fill finds the non-selected voxels ridge spheres reach:
         BM_SITES_AUTO (0), BM_SITES_SPHERES (1) or BM_SITES_CHAINS (2)."""
         self.call("bm_ctx_set_site_method", int(method))
+
+    def set_fill_tile_rows(self, rows: int = 0) -> None:
+        """Rows of y in the sphere fill's tiles: 0 (by volume size), 32 or 64."""
+        self.call("bm_ctx_set_fill_tile_rows", int(rows))
 
     def set_wait_cycles(self, cycles: int = -1) -> None:
         """Cycle limit of the device-side bounded waits (-1: the default, ~2 s;

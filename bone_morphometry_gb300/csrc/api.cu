@@ -194,7 +194,8 @@ uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, u
   FillInfo hi;
   check(ctx, cudaMemcpyAsync(&hi, info, sizeof hi, cudaMemcpyDeviceToHost, s), "fill info readback");
   check(ctx, cudaStreamSynchronize(s), "rank kernel");
-  const long long tiles = fill_tile_count(dm);
+  const int ty = fill_tile_rows(dm, ctx->fill_rows);
+  const long long tiles = fill_tile_count(dm, ty);
   const long long nbins = tiles * (long long)hi.nR;
   uint32_t* counts = static_cast<uint32_t*>(ensure(ctx, ctx->bincounts, ((size_t)nbins + 1) * 4, "bin counts"));
   uint32_t* offsets = static_cast<uint32_t*>(ensure(ctx, ctx->binoffsets, ((size_t)nbins + 1) * 4, "bin offsets"));
@@ -202,7 +203,8 @@ uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, u
   check(ctx, cudaMemsetAsync(counts, 0, ((size_t)nbins + 1) * 4, s), "memset");
   if (hi.nR > 0) {
     timed(ctx, KF_FILL_BIN, s, "bin count kernel", [&] {
-      return launch_bin(true, ridges, ctr, max_ridges, rank, info, dm, counts, nullptr, nullptr, s, &ctx->launches);
+      return launch_bin(true, ridges, ctr, max_ridges, rank, info, dm, ty, counts, nullptr, nullptr, s,
+                        &ctx->launches);
     });
   }
   timed(ctx, KF_FILL_BIN, s, "bin scan",
@@ -219,7 +221,8 @@ uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, u
       ensure(ctx, ctx->binentries, ((size_t)hi.total_entries + 1) * 4, "bin entries"));
   if (hi.nR > 0) {
     timed(ctx, KF_FILL_BIN, s, "bin scatter kernel", [&] {
-      return launch_bin(false, ridges, ctr, max_ridges, rank, info, dm, counts, offsets, entries, s, &ctx->launches);
+      return launch_bin(false, ridges, ctr, max_ridges, rank, info, dm, ty, counts, offsets, entries, s,
+                        &ctx->launches);
     });
   }
   // Sites: the site kernel's half-warp steps over the ridge spheres' lattice
@@ -243,9 +246,9 @@ uint32_t* fill_phase(bm_ctx* ctx, Dims dm, const uint2* ridges, Counters* ctr, u
   } else {
     ensure_surf(ctx, rmax);
   }
-  uint32_t* order = static_cast<uint32_t*>(ensure(ctx, ctx->tileorder, tile_order_words(dm) * 4, "tile order"));
+  uint32_t* order = static_cast<uint32_t*>(ensure(ctx, ctx->tileorder, tile_order_words(dm, ty) * 4, "tile order"));
   timed(ctx, KF_FILL, s, "tile fill kernel", [&] {
-    return launch_tile_fill(entries, offsets, rvals, rgeo, info, selbits, dm, order, F, s, &ctx->launches);
+    return launch_tile_fill(entries, offsets, rvals, rgeo, info, selbits, dm, ty, order, F, s, &ctx->launches);
   });
   if (chains) {
     timed(ctx, KF_FILL_SITES, s, "chain y pass",
@@ -727,6 +730,7 @@ bm_ctx* twin_of(bm_ctx* ctx) {
   if (st != BM_OK) fail(ctx, st, "second stream context creation failed");
   t->profiling = ctx->profiling;
   t->site_method = ctx->site_method;
+  t->fill_rows = ctx->fill_rows;
   t->wait_cycles = ctx->wait_cycles;
   ctx->twin = t;
   return t;
@@ -1086,6 +1090,16 @@ int bm_ctx_set_site_method(bm_ctx* ctx, int method) {
       fail(ctx, BM_ERR_INVALID, "site method must be 0 (auto), 1 (spheres) or 2 (chains); got %d", method);
     ctx->site_method = method;
     if (ctx->twin) ctx->twin->site_method = method;
+    return BM_OK;
+  });
+}
+
+int bm_ctx_set_fill_tile_rows(bm_ctx* ctx, int rows) {
+  return guarded(ctx, [&]() -> int {
+    if (rows != 0 && rows != 32 && rows != 64)
+      fail(ctx, BM_ERR_INVALID, "fill tile rows must be 0 (by volume size), 32 or 64; got %d", rows);
+    ctx->fill_rows = rows;
+    if (ctx->twin) ctx->twin->fill_rows = rows;
     return BM_OK;
   });
 }

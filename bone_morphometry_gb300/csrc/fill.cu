@@ -120,6 +120,7 @@ __global__ void rank_finalize_kernel(const uint32_t* __restrict__ occ, uint32_t*
 struct Geom {
   int ntx, nty, ntz;
   long long ntiles;
+  int ty;  // rows of y per tile (32 or 64)
 };
 
 
@@ -144,13 +145,13 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
     const uint32_t rank = rank_desc[R];
     steps += ((unsigned)rad * 402u + 1023u) >> 10;  // ceil(2 pi rad / 16): 2 pi / 16 ~ 402 / 1024
     const int tx0 = max(x - rad, 0) / kFillTX, tx1 = min(x + rad, dm.w - 1) / kFillTX;
-    const int ty0 = max(y - rad, 0) / kFillTY, ty1 = min(y + rad, dm.h - 1) / kFillTY;
+    const int ty0 = max(y - rad, 0) / g.ty, ty1 = min(y + rad, dm.h - 1) / g.ty;
     const int tz0 = max(z - rad, 0) / kFillTZ, tz1 = min(z + rad, dm.d - 1) / kFillTZ;
     for (int tz = tz0; tz <= tz1; ++tz) {
       const int bz0 = tz * kFillTZ, bz1 = bz0 + kFillTZ - 1;
       const long long ddz = z < bz0 ? bz0 - z : (z > bz1 ? z - bz1 : 0);
       for (int ty = ty0; ty <= ty1; ++ty) {
-        const int by0 = ty * kFillTY, by1 = by0 + kFillTY - 1;
+        const int by0 = ty * g.ty, by1 = by0 + g.ty - 1;
         const long long ddy = y < by0 ? by0 - y : (y > by1 ? y - by1 : 0);
         const long long dyz = ddz * ddz + ddy * ddy;
         if (dyz > (long long)R) continue;
@@ -185,60 +186,81 @@ bin_kernel(const uint2* __restrict__ ridges, const Counters* __restrict__ ctr, c
 
 constexpr int kFillThreads = 256;
 constexpr int kFillWarps = kFillThreads / 32;
-constexpr int kRows = kFillTZ * kFillTY;  // 1024 rows of 32 voxels per tile
 
 __device__ __forceinline__ uint32_t range_mask(int a, int b) {  // bits a..b, 0 <= a <= b <= 31
   return (0xffffffffu >> (31 - b)) & (0xffffffffu << a);
 }
 
-// Word of row (z, y) in the unpainted-voxel masks: rotated by 3z within the
-// plane, so that threads reading the same y of consecutive planes (the planes
-// of one ball) fall into different banks.
-__device__ __forceinline__ int urow(int z, int y) { return z * kFillTY + ((y + 3 * z) & (kFillTY - 1)); }
+// Word of row (z, y) in the unpainted-voxel masks of a tile with TY rows per
+// plane: rotated by 3z within the plane, so that threads reading the same y of
+// consecutive planes (the planes of one ball) fall into different banks.
+template <int TY>
+__device__ __forceinline__ int urow(int z, int y) { return z * TY + ((y + 3 * z) & (TY - 1)); }
 
 constexpr int kBinChunk = 256;    // bins whose offsets are staged in shared memory at a time
 constexpr int kEntWin = 768;      // ball entries staged in shared memory at a time
 constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 rows (level 0 is usel itself);
                                   // two 32-row lookups cover a plane's 64 rows
 constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
-constexpr int kRotStride = 65;    // words per range-OR row: lanes testing different planes hit different banks
-constexpr int kItems = 2048;      // (ball, plane) paint items per round
-constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
-// a paint item packs (window index << 16) | (rows - 1) << 10 | first row << 4 | plane
-static_assert(kEntWin <= (1 << 16) && kFillTY <= 64 && kFillTZ <= 16, "paint item encoding");
 
-// rot[lv - 1][z][y] (rows of kRotStride words) = OR of the unpainted-voxel
-// masks of rows y .. y + 2^lv - 1 of plane z (rows past the tile edge count
-// as empty), lv = 1 .. 5.  Built with shuffles, one plane per warp step; lane
-// l holds rows l and l + 32.
+// The tile shape: 32 x TY x 16 voxels, TY = 32 or 64 rows of y.  Taller tiles
+// give fewer ball entries and plane tests per voxel, shorter ones more tiles
+// (a small volume's fill is bound by its tiles' serial chains of r^2 bins).
+template <int TY>
+struct FillTile {
+  static_assert(TY == 32 || TY == 64, "32 or 64 rows per tile");
+  static constexpr int kRows = kFillTZ * TY;
+  static constexpr int kRotStride = TY + 1;  // words per range-OR row: lanes on different planes hit different banks
+  // (ball, plane) paint items per round: as many as 5 CTAs per SM leave room for
+  static constexpr int kItems = TY == 32 ? 4096 : 2048;
+  static constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
+  static constexpr size_t kSmemWords = (size_t)kRows + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
+                                       (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130;
+};
+// a paint item packs (window index << 16) | (rows - 1) << 10 | first row << 4 | plane
+static_assert(kEntWin <= (1 << 16) && kFillTZ <= 16, "paint item encoding (and rows per tile <= 64)");
+
+// rot[lv - 1][z][y] (rows of TY + 1 words) = OR of the unpainted-voxel masks
+// of rows y .. y + 2^lv - 1 of plane z (rows past the tile edge count as
+// empty), lv = 1 .. 5.  Built with shuffles, one plane per warp step; lane l
+// holds row l (and l + 32 in 64-row tiles).
+template <int TY>
 __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uint32_t* __restrict__ rot, int warp,
                                           int lane, int nwarps) {
-  static_assert(kFillTY == 64, "two rows per lane");
+  constexpr int kStride = FillTile<TY>::kRotStride;
   for (int zz = warp; zz < kFillTZ; zz += nwarps) {
-    uint32_t v0 = usel[urow(zz, lane)], v1 = usel[urow(zz, lane + 32)];
+    if constexpr (TY == 64) {
+      uint32_t v0 = usel[urow<TY>(zz, lane)], v1 = usel[urow<TY>(zz, lane + 32)];
 #pragma unroll
-    for (int lv = 1; lv < kRotLevels; ++lv) {
-      const int s = 1 << (lv - 1);  // row y takes the previous level's rows y and y + s
-      const uint32_t a = __shfl_sync(0xffffffffu, v0, (lane + s) & 31);
-      const uint32_t b = __shfl_sync(0xffffffffu, v1, (lane + s) & 31);
-      const bool lo = lane + s < 32;
-      v0 |= lo ? a : b;
-      v1 |= lo ? b : 0u;
-      uint32_t* rr = rot + ((lv - 1) * kFillTZ + zz) * kRotStride;
-      rr[lane] = v0;
-      rr[lane + 32] = v1;
+      for (int lv = 1; lv < kRotLevels; ++lv) {
+        const int s = 1 << (lv - 1);  // row y takes the previous level's rows y and y + s
+        const uint32_t a = __shfl_sync(0xffffffffu, v0, (lane + s) & 31);
+        const uint32_t b = __shfl_sync(0xffffffffu, v1, (lane + s) & 31);
+        const bool lo = lane + s < 32;
+        v0 |= lo ? a : b;
+        v1 |= lo ? b : 0u;
+        uint32_t* rr = rot + ((lv - 1) * kFillTZ + zz) * kStride;
+        rr[lane] = v0;
+        rr[lane + 32] = v1;
+      }
+    } else {
+      uint32_t v = usel[urow<TY>(zz, lane)];
+#pragma unroll
+      for (int lv = 1; lv < kRotLevels; ++lv) {
+        const uint32_t u = __shfl_down_sync(0xffffffffu, v, 1 << (lv - 1));
+        v |= (lane + (1 << (lv - 1)) < 32) ? u : 0u;
+        rot[((lv - 1) * kFillTZ + zz) * kStride + lane] = v;
+      }
     }
   }
 }
 
-constexpr size_t kTileFillSmemWords = (size_t)kRows + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
-                                      (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130;
-
-// One CTA per tile (32 x 64 x 16 voxels) paints the tile's selected voxels.
+// One CTA per tile (32 x TY x 16 voxels) paints the tile's selected voxels.
 // A painted voxel's r^2 goes straight to the map (each selected voxel is
 // painted once: its bit in usel is cleared atomically first), and the voxels
 // left unpainted get 0 at the end; without a per-voxel value array the CTA
-// needs 44 KB of shared memory, and 5 CTAs share an SM (48 registers).
+// needs 37 KB (32 rows) or 44 KB (64 rows) of shared memory, and 5 CTAs share
+// an SM (48 registers).
 // Shared memory:
 //   sown : per row (z, y), the tile's selected voxels;
 //   usel : per row (z, y), the selected voxels not yet painted;
@@ -261,11 +283,16 @@ constexpr size_t kTileFillSmemWords = (size_t)kRows + kRows + (kBinChunk + 4) + 
 // bin have the same r^2, so the order of their items does not matter (two
 // threads may write the same value).  Non-selected voxels are left 0 here;
 // the site pass or the chain passes add the ones a sphere reaches.
+template <int TY>
 __global__ void __launch_bounds__(kFillThreads, 5)
 tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restrict__ offsets,
                  const uint32_t* __restrict__ rvals, const uint4* __restrict__ rgeo, const FillInfo* __restrict__ info,
                  const uint32_t* __restrict__ selbits, Dims dm, VoxelDecoder vd, Geom g,
                  const uint32_t* __restrict__ order, uint32_t* __restrict__ fillmap) {
+  constexpr int kRows = FillTile<TY>::kRows;
+  constexpr int kRotStride = FillTile<TY>::kRotStride;
+  constexpr int kItems = FillTile<TY>::kItems;
+  constexpr int kRound = FillTile<TY>::kRound;
   extern __shared__ uint32_t smem[];
   uint32_t* sown = smem;                                     // kRows: the tile's selected voxels per row
   uint32_t* usel = smem + kRows;                             // kRows
@@ -291,13 +318,13 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
     const int tx = (int)(tile % g.ntx);
     const int ty = (int)((tile / g.ntx) % g.nty);
     const int tz = (int)(tile / ((long long)g.ntx * g.nty));
-    const int x0 = tx * kFillTX, y0 = ty * kFillTY, z0 = tz * kFillTZ;
-    const int vx = min(kFillTX, dm.w - x0), vy = min(kFillTY, dm.h - y0), vz = min(kFillTZ, dm.d - z0);
+    const int x0 = tx * kFillTX, y0 = ty * TY, z0 = tz * kFillTZ;
+    const int vx = min(kFillTX, dm.w - x0), vy = min(TY, dm.h - y0), vz = min(kFillTZ, dm.d - z0);
     const uint32_t xmask = vx >= 32 ? 0xffffffffu : ((1u << vx) - 1u);
     const uint32_t* off = offsets + tile * (long long)nR;
     if (off[0] == off[nR]) {  // no ball reaches this tile: all zero
       for (int r = warp; r < kRows; r += kFillWarps) {
-        const int zz = r / kFillTY, yy = r % kFillTY;
+        const int zz = r / TY, yy = r % TY;
         if (zz < vz && yy < vy && lane < vx)
           fillmap[((long long)(z0 + zz) * dm.h + (y0 + yy)) * dm.w + x0 + lane] = 0u;
       }
@@ -312,22 +339,22 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
     parity = 0;
     bool any_sel = false;
     for (int r = tid; r < kRows; r += kFillThreads) {
-      const int zz = r / kFillTY, yy = r % kFillTY;
+      const int zz = r / TY, yy = r % TY;
       uint32_t own = 0u;
       if (zz < vz && yy < vy) own = selbits[((long long)(z0 + zz) * dm.h + (y0 + yy)) * nw + tx] & xmask;
-      usel[urow(zz, yy)] = own;
-      sown[urow(zz, yy)] = own;
+      usel[urow<TY>(zz, yy)] = own;
+      sown[urow<TY>(zz, yy)] = own;
       any_sel = any_sel || own != 0u;
     }
     if (!__syncthreads_or(any_sel)) {  // nothing selected here (outside the ROI, say): all zero
       for (int r = warp; r < kRows; r += kFillWarps) {
-        const int zz = r / kFillTY, yy = r % kFillTY;
+        const int zz = r / TY, yy = r % TY;
         if (zz < vz && yy < vy && lane < vx)
           fillmap[((long long)(z0 + zz) * dm.h + (y0 + yy)) * dm.w + x0 + lane] = 0u;
       }
       continue;
     }
-    build_rot(usel, rot, warp, lane, kFillWarps);
+    build_rot<TY>(usel, rot, warp, lane, kFillWarps);
     for (uint32_t b0 = 0; b0 < nR; b0 += kBinChunk) {
       const uint32_t nb = min((uint32_t)kBinChunk, nR - b0);
       __syncthreads();
@@ -366,7 +393,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
         const uint32_t e = boff[bl + 1];
         // this bin's disk radii: hyt[|dz|] = isqrt(r2 - dz^2)
         for (int i = tid; i <= rad; i += kFillThreads) hyt[i] = (uint16_t)isqrt24((uint32_t)(R - i * i));
-        if (k % kRotEvery == 0 && k > 0) build_rot(usel, rot, warp, lane, kFillWarps);
+        if (k % kRotEvery == 0 && k > 0) build_rot<TY>(usel, rot, warp, lane, kFillWarps);
         __syncthreads();
         for (uint32_t ss = boff[bl]; ss < e;) {
           if (ss < s_wlo || ss >= s_whi) {  // reload the entry window at ss (uniform decision)
@@ -404,10 +431,10 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             const int xa = max(cx - hy, 0), xb = min(cx + hy, vx - 1);
             ok = ok && pya <= pyb && xa <= xb;
             const int zc = min(zz, kFillTZ - 1);
-            const int ya = min(pya, kFillTY - 1), yb = max(min(pyb, kFillTY - 1), ya);
+            const int ya = min(pya, TY - 1), yb = max(min(pyb, TY - 1), ya);
             const int lv = min(31 - __clz(yb - ya + 1), kRotLevels - 1);  // 2^lv <= span: two lookups cover it
             const uint32_t* tl = rot + (max(lv - 1, 0) * kFillTZ + zc) * kRotStride;
-            const uint32_t orr = lv == 0 ? usel[urow(zc, ya)] : (tl[ya] | tl[yb - (1 << lv) + 1]);
+            const uint32_t orr = lv == 0 ? usel[urow<TY>(zc, ya)] : (tl[ya] | tl[yb - (1 << lv) + 1]);
             return ok && (orr & range_mask(min(max(xa, 0), 31), max(min(xb, 31), min(max(xa, 0), 31)))) != 0u;
           };
           // items: (window index, rows ya .. ya + n, plane)
@@ -449,7 +476,7 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
             const int hw = (int)hyt[abs(dz)];
             const uint32_t wide = range_mask(max(bx - hw, 0), min(bx + hw, vx - 1));
             for (int y = ya + sub; y <= yb; y += G) {
-              const int row = urow(zz, y);
+              const int row = urow<TY>(zz, y);
               const uint32_t m = usel[row] & wide;
               if (!m) continue;
               const int dy = y - by;
@@ -479,8 +506,8 @@ tile_fill_kernel(const uint32_t* __restrict__ entries, const uint32_t* __restric
     // the voxels no ball painted (non-selected ones; the site pass adds those
     // a sphere reaches) get 0: one row per warp step
     for (int r = warp; r < kRows; r += kFillWarps) {
-      const int zz = r / kFillTY, yy = r % kFillTY;
-      const uint32_t painted = sown[urow(zz, yy)] & ~usel[urow(zz, yy)];
+      const int zz = r / TY, yy = r % TY;
+      const uint32_t painted = sown[urow<TY>(zz, yy)] & ~usel[urow<TY>(zz, yy)];
       if (zz < vz && yy < vy && lane < vx && !((painted >> lane) & 1u))
         fillmap[((long long)(z0 + zz) * dm.h + (y0 + yy)) * dm.w + x0 + lane] = 0u;
     }
@@ -580,10 +607,11 @@ surf_kernel(uint32_t lo, uint32_t hi, uint32_t* __restrict__ surf_cnt, const uin
   }
 }
 
-Geom geom_of(Dims dm) {
+Geom geom_of(Dims dm, int ty) {
   Geom g;
+  g.ty = ty;
   g.ntx = (dm.w + kFillTX - 1) / kFillTX;
-  g.nty = (dm.h + kFillTY - 1) / kFillTY;
+  g.nty = (dm.h + ty - 1) / ty;
   g.ntz = (dm.d + kFillTZ - 1) / kFillTZ;
   g.ntiles = (long long)g.ntx * g.nty * g.ntz;
   return g;
@@ -598,7 +626,12 @@ inline unsigned blocks_for(long long work, int per_block, long long cap) {
 
 }  // namespace
 
-long long fill_tile_count(Dims dm) { return geom_of(dm).ntiles; }
+int fill_tile_rows(Dims dm, int requested) {
+  if (requested == 32 || requested == 64) return requested;
+  return dm.n() >= kFillTallMinVoxels ? 64 : 32;
+}
+
+long long fill_tile_count(Dims dm, int ty) { return geom_of(dm, ty).ntiles; }
 
 size_t scan_scratch_words(long long n) {
   size_t words = 0;
@@ -636,9 +669,9 @@ cudaError_t launch_rank(const uint32_t* occ, uint32_t* rank_desc, uint32_t rmax,
 }
 
 cudaError_t launch_bin(bool count, const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
-                       const uint32_t* rank_desc, FillInfo* info, Dims dm, uint32_t* counts,
+                       const uint32_t* rank_desc, FillInfo* info, Dims dm, int ty, uint32_t* counts,
                        const uint32_t* offsets, uint32_t* entries, cudaStream_t s, unsigned long long* launches) {
-  const Geom g = geom_of(dm);
+  const Geom g = geom_of(dm, ty);
   const unsigned blocks = blocks_for((long long)max_ridges, 256, 152 * 32);
   if (count)
     bin_kernel<true><<<blocks, 256, 0, s>>>(ridges, ctr, rank_desc, info, dm, VoxelDecoder::of(dm), g, counts,
@@ -713,15 +746,28 @@ __global__ void tile_weight_scatter_kernel(const uint32_t* __restrict__ offsets,
 
 }  // namespace
 
-size_t tile_order_words(Dims dm) { return (size_t)geom_of(dm).ntiles + kOrderBuckets; }
+size_t tile_order_words(Dims dm, int ty) { return (size_t)geom_of(dm, ty).ntiles + kOrderBuckets; }
+
+namespace {
+template <int TY>
+cudaError_t launch_tile_fill_rows(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
+                                  const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm,
+                                  const Geom& g, const uint32_t* order, uint32_t* fillmap, cudaStream_t s) {
+  const size_t smem = FillTile<TY>::kSmemWords * sizeof(uint32_t);
+  cudaError_t e = cudaFuncSetAttribute(tile_fill_kernel<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const long long grid = g.ntiles < (1LL << 31) - 1 ? g.ntiles : (1LL << 31) - 1;
+  tile_fill_kernel<TY><<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, rgeo, info, selbits, dm,
+                                                                   VoxelDecoder::of(dm), g, order, fillmap);
+  return cudaGetLastError();
+}
+}  // namespace
 
 cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
-                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm,
+                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm, int ty,
                              uint32_t* order_scratch, uint32_t* fillmap, cudaStream_t s, unsigned long long* launches) {
-  const Geom g = geom_of(dm);
-  const size_t smem = kTileFillSmemWords * sizeof(uint32_t);
-  cudaError_t e = cudaFuncSetAttribute(tile_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  const Geom g = geom_of(dm, ty);
+  cudaError_t e;
   uint32_t* hist = order_scratch;
   uint32_t* order = order_scratch + kOrderBuckets;
   e = cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(uint32_t), s);
@@ -730,10 +776,10 @@ cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, c
   tile_weight_hist_kernel<<<ob, 256, 0, s>>>(offsets, info, g.ntiles, hist);
   tile_weight_scan_kernel<<<1, 1, 0, s>>>(hist);
   tile_weight_scatter_kernel<<<ob, 256, 0, s>>>(offsets, info, g.ntiles, hist, order);
-  const long long grid = g.ntiles < (1LL << 31) - 1 ? g.ntiles : (1LL << 31) - 1;
-  tile_fill_kernel<<<(unsigned)grid, kFillThreads, smem, s>>>(entries, offsets, rvals, rgeo, info, selbits, dm,
-                                                               VoxelDecoder::of(dm), g, order, fillmap);
+  e = ty == 64 ? launch_tile_fill_rows<64>(entries, offsets, rvals, rgeo, info, selbits, dm, g, order, fillmap, s)
+              : launch_tile_fill_rows<32>(entries, offsets, rvals, rgeo, info, selbits, dm, g, order, fillmap, s);
   *launches += 4;
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

@@ -88,7 +88,11 @@ cudaError_t launch_cleanup(const uint32_t* fillmap, const uint32_t* selbits, Dim
 cudaError_t launch_dia_table(const uint4* lut, uint32_t n, float* dia, cudaStream_t s, unsigned long long* launches);
 
 // Tile-owned fill (fill.cu).
-long long fill_tile_count(Dims dm);
+// Rows of y per fill tile: 64 for volumes of at least kFillTallMinVoxels (fewer
+// ball entries per voxel), else 32 (more tiles: a small volume's fill is bound
+// by its tiles' serial chains); requested = 32 or 64 forces it.
+int fill_tile_rows(Dims dm, int requested);
+long long fill_tile_count(Dims dm, int ty);
 size_t scan_scratch_words(long long n);
 // Exclusive scan of n u32 values (out may alias in); scratch of scan_scratch_words(n).
 cudaError_t launch_scan(const uint32_t* in, uint32_t* out, long long n, uint32_t* scratch, cudaStream_t s,
@@ -97,18 +101,19 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, long long n, uint32_t
 // rgeo[rank] = {r2, ceil sqrt, floor sqrt, 0} for every rank.
 cudaError_t launch_rank(const uint32_t* occ, uint32_t* rank_desc, uint32_t rmax, uint32_t* rvals, uint4* rgeo,
                         FillInfo* info, uint32_t* scan_scratch, cudaStream_t s, unsigned long long* launches);
+// ty: the fill tile's rows of y (fill_tile_rows).
 cudaError_t launch_bin(bool count, const uint2* ridges, const Counters* ctr, unsigned long long max_ridges,
-                       const uint32_t* rank_desc, FillInfo* info, Dims dm, uint32_t* counts,
+                       const uint32_t* rank_desc, FillInfo* info, Dims dm, int ty, uint32_t* counts,
                        const uint32_t* offsets, uint32_t* entries, cudaStream_t s, unsigned long long* launches);
 // Sphere lattice-point table: count (surf_cnt[r2]) or fill (surf_pts from surf_off[r2]) for r2 in [lo, hi].
 cudaError_t launch_surf(bool count, uint32_t lo, uint32_t hi, uint32_t* surf_cnt, const uint32_t* surf_off,
                         uint32_t* surf_pts, cudaStream_t s, unsigned long long* launches);
 // Selected voxels of every tile from the binned balls; non-selected voxels get 0.
 // selbits: the phase's row-padded selection bitmask (edt_x output).
-// order_scratch: tile_order_words(dm) words (the tiles' processing order).
-size_t tile_order_words(Dims dm);
+// order_scratch: tile_order_words(dm, ty) words (the tiles' processing order).
+size_t tile_order_words(Dims dm, int ty);
 cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, const uint32_t* rvals,
-                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm,
+                             const uint4* rgeo, const FillInfo* info, const uint32_t* selbits, Dims dm, int ty,
                              uint32_t* order_scratch, uint32_t* fillmap, cudaStream_t s, unsigned long long* launches);
 // Non-selected voxels on each ridge's sphere: atomic max of r2 (after the tile
 // fill).  surf_off / surf_pts: the lattice-point table covering every ridge r2;

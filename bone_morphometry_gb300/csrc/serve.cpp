@@ -77,8 +77,11 @@ void copy_message(bm_result& r, const char* msg) {
 // Settings every worker context takes from the pool (no effect on results).
 struct PoolSettings {
   int site_method = BM_SITES_AUTO;
+  int fill_rows = 0;
   bool split_phases = true;
-  bool operator==(const PoolSettings& o) const { return site_method == o.site_method && split_phases == o.split_phases; }
+  bool operator==(const PoolSettings& o) const {
+    return site_method == o.site_method && fill_rows == o.fill_rows && split_phases == o.split_phases;
+  }
 };
 
 class Pool {
@@ -93,6 +96,7 @@ class Pool {
         break;
       }
       c->site_method = settings.site_method;
+      c->fill_rows = settings.fill_rows;
       c->split_phases = settings.split_phases;
       ctxs_.push_back(c);
     }
@@ -319,9 +323,10 @@ int bm_batch_tbth_tbsp(bm_ctx* ctx, const bm_specimen* items, size_t n, int devi
                        bm_stats* thickness, bm_stats* spacing, int* status) {
   if (!ctx || (n && !items)) return BM_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->pool_mu);
-  // the workers take the context's site method and phase scheduling
+  // the workers take the context's site method, fill tile rows and phase scheduling
   PoolSettings want;
   want.site_method = ctx->site_method;
+  want.fill_rows = ctx->fill_rows;
   want.split_phases = ctx->split_phases;
   if (ctx->pool && !(ctx->pool->settings() == want)) {
     pool_destroy(ctx->pool);

@@ -73,26 +73,32 @@ def batch_tbth_tbsp(specimens, feature_mode=FeatureMode.CLASSIC, ctx: Context | 
 
 # ---- settings of the batched form, picked by measurement ----------------------------------
 #
-# Three settings change how fast a batch runs and never what it returns: the
+# Four settings change how fast a batch runs and never what it returns: the
 # number of workers, how the fill finds the non-selected voxels that ridge
 # spheres reach (the sphere lattice points, a scatter per ridge, or the chain
 # passes, a gather along the distance transform's argmins; local_thickness.rs:169-202
-# paints them too), and whether each specimen's two phases run side by side.
-# The tuner runs the whole batch once per candidate and keeps the fastest,
-# per GPU and per mix of specimen sizes, in a JSON file, so a later batch of the
-# same kind starts from the stored choice.
+# paints them too), the fill's tile shape (32 x 32 x 16 or 32 x 64 x 16 voxels),
+# and whether each specimen's two phases run side by side.  The tuner runs the
+# whole batch for every candidate and keeps the fastest, per GPU and per mix of
+# specimen sizes, in a JSON file, so a later batch of the same kind starts from
+# the stored choice.
 
-TUNE_CANDIDATES = tuple((w, m, c) for w in (2, 4, 6, 8, 12) for m in (BM_SITES_AUTO, BM_SITES_SPHERES, BM_SITES_CHAINS)
-                        for c in (True, False))
+TUNE_CANDIDATES = tuple((w, m, r, c) for w in (4, 6, 8) for m in (BM_SITES_AUTO, BM_SITES_SPHERES, BM_SITES_CHAINS)
+                        for r in (32, 64) for c in (True, False))
+_TUNE_FIELDS = ("workers", "site_method", "fill_tile_rows", "concurrent_phases")
 
 
 @dataclass
 class Tuning:
     workers: int
     site_method: int
+    fill_tile_rows: int
     concurrent_phases: bool
     batch_ms: float          # the chosen candidate's time when it was measured
     from_cache: bool = False
+
+    def setting(self):
+        return (self.workers, self.site_method, self.fill_tile_rows, self.concurrent_phases)
 
 
 def tuning_cache_path() -> str:
@@ -140,7 +146,7 @@ def _save_cache(path: str, data: dict) -> None:
 
 def autotune(run, key: str, path: str, candidates=TUNE_CANDIDATES, retune: bool = False,
              clock=time.perf_counter, repeats: int = 3):
-    """run(workers, site_method, concurrent_phases) -> results.  On a cache
+    """run(workers, site_method, fill_tile_rows, concurrent_phases) -> results.  On a cache
     miss (or retune) every candidate runs once untimed (a new setting gives
     the pool new worker contexts, whose buffers grow on their first batch),
     then `repeats` times timed; the candidate with the lowest median time is
@@ -148,10 +154,10 @@ def autotune(run, key: str, path: str, candidates=TUNE_CANDIDATES, retune: bool 
     hit only the stored candidate runs.  Returns (results, Tuning)."""
     cache = _load_cache(path)
     hit = cache.get(key)
-    if hit is not None and not retune:
-        t = Tuning(int(hit["workers"]), int(hit["site_method"]), bool(hit["concurrent_phases"]),
-                   float(hit["batch_ms"]), True)
-        return run(t.workers, t.site_method, t.concurrent_phases), t
+    if hit is not None and all(f in hit for f in _TUNE_FIELDS) and not retune:
+        t = Tuning(int(hit["workers"]), int(hit["site_method"]), int(hit["fill_tile_rows"]),
+                   bool(hit["concurrent_phases"]), float(hit["batch_ms"]), True)
+        return run(*t.setting()), t
     best = None
     for cand in candidates:
         run(*cand)  # warm-up of this setting
@@ -163,10 +169,9 @@ def autotune(run, key: str, path: str, candidates=TUNE_CANDIDATES, retune: bool 
         dt = sorted(times)[len(times) // 2]
         if best is None or dt < best[0]:
             best = (dt, cand, res)
-    dt, (w, m, c), res = best
-    t = Tuning(int(w), int(m), bool(c), 1e3 * dt)
-    cache[key] = {"workers": t.workers, "site_method": t.site_method, "concurrent_phases": t.concurrent_phases,
-                  "batch_ms": round(t.batch_ms, 3)}
+    dt, (w, m, r, c), res = best
+    t = Tuning(int(w), int(m), int(r), bool(c), 1e3 * dt)
+    cache[key] = dict(zip(_TUNE_FIELDS, t.setting()), batch_ms=round(t.batch_ms, 3))
     _save_cache(path, cache)
     return res, t
 
@@ -179,9 +184,10 @@ def tuned_batch_tbth_tbsp(specimens, feature_mode=FeatureMode.CLASSIC, ctx: Cont
     items = list(specimens)
     key = device_key(ctx.device) + "|" + mix_signature([tuple(sp.bone.shape) for sp in items])
 
-    def run(workers, site_method, concurrent):
+    def run(workers, site_method, fill_rows, concurrent):
         ctx.call("bm_ctx_set_workers", int(workers))
         ctx.set_site_method(site_method)
+        ctx.set_fill_tile_rows(fill_rows)
         ctx.set_concurrent_phases(concurrent)
         return batch_tbth_tbsp(items, feature_mode, ctx)
 

@@ -207,9 +207,9 @@ typedef struct bm_specimen {
 /* Tb.Th / Tb.Sp of n specimens of uneven sizes.  The context's worker pool
  * (bm_ctx_set_workers; by default 4 workers, each with its own stream and
  * buffers) takes specimens as workers free up, so their kernels overlap on the
- * GPU.  The workers take the context's site method and phase scheduling
- * (bm_ctx_set_site_method, bm_ctx_set_concurrent_phases; the pool is recreated
- * when they change).  Per-specimen results and statuses go to thickness[i],
+ * GPU.  The workers take the context's site method, fill tile rows and phase
+ * scheduling (bm_ctx_set_site_method, bm_ctx_set_fill_tile_rows,
+ * bm_ctx_set_concurrent_phases; the pool is recreated when they change).  Per-specimen results and statuses go to thickness[i],
  * spacing[i], status[i]; the call returns BM_OK when every specimen succeeded,
  * else the first non-zero status (the others still complete).
  * device_pointers != 0: bone/roi are device pointers on the context's device. */
@@ -294,6 +294,12 @@ int bm_ctx_set_concurrent_phases(bm_ctx* ctx, int on);
  * identical either way. */
 enum { BM_SITES_AUTO = 0, BM_SITES_SPHERES = 1, BM_SITES_CHAINS = 2 };
 int bm_ctx_set_site_method(bm_ctx* ctx, int method);
+
+/* Rows of y in the sphere fill's tiles (32 x rows x 16 voxels): 0 (the
+ * default) picks 64 for volumes of at least 2^26 voxels (fewer ball entries
+ * and plane tests per voxel) and 32 below (more tiles, shorter serial chains);
+ * 32 or 64 forces it.  Results are identical either way. */
+int bm_ctx_set_fill_tile_rows(bm_ctx* ctx, int rows);
 
 /* Cycle limit of the device-side bounded waits of this context's kernels (the
  * TMA-staged y pass waits on its copy's mbarrier): cycles < 0 restores the

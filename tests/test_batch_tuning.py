@@ -19,13 +19,13 @@ class FakeBatch:
     def clock(self):
         return self.now
 
-    def run(self, w, m, c):
-        self.calls.append((w, m, c))
-        self.now += self.cost[(w, m, c)]
+    def run(self, *cand):
+        self.calls.append(cand)
+        self.now += self.cost[cand]
         return ["result"]
 
 
-CANDS = ((2, BM_SITES_AUTO, True), (4, BM_SITES_SPHERES, False), (8, BM_SITES_CHAINS, True))
+CANDS = ((2, BM_SITES_AUTO, 32, True), (4, BM_SITES_SPHERES, 64, False), (8, BM_SITES_CHAINS, 32, True))
 
 
 def test_picks_the_fastest_and_persists(tmp_path):
@@ -33,12 +33,12 @@ def test_picks_the_fastest_and_persists(tmp_path):
     fb = FakeBatch({CANDS[0]: 0.30, CANDS[1]: 0.10, CANDS[2]: 0.20})
     res, t = SV.autotune(fb.run, "gpu|mix", path, CANDS, clock=fb.clock)
     assert res == ["result"]
-    assert (t.workers, t.site_method, t.concurrent_phases) == (4, BM_SITES_SPHERES, False)
+    assert t.setting() == (4, BM_SITES_SPHERES, 64, False)
     assert abs(t.batch_ms - 100.0) < 1e-9 and not t.from_cache
     assert fb.calls == [c for c in CANDS for _ in range(4)]  # each candidate: a warm-up, then three timed runs
     stored = json.load(open(path))
-    assert stored == {"gpu|mix": {"workers": 4, "site_method": BM_SITES_SPHERES, "concurrent_phases": False,
-                                  "batch_ms": 100.0}}
+    assert stored == {"gpu|mix": {"workers": 4, "site_method": BM_SITES_SPHERES, "fill_tile_rows": 64,
+                                  "concurrent_phases": False, "batch_ms": 100.0}}
 
 
 def test_cache_hit_runs_only_the_stored_candidate(tmp_path):
@@ -47,7 +47,7 @@ def test_cache_hit_runs_only_the_stored_candidate(tmp_path):
     SV.autotune(fb.run, "k", path, CANDS, clock=fb.clock)
     fb.calls.clear()
     res, t = SV.autotune(fb.run, "k", path, CANDS, clock=fb.clock)
-    assert t.from_cache and (t.workers, t.site_method, t.concurrent_phases) == CANDS[2]
+    assert t.from_cache and t.setting() == CANDS[2]
     assert fb.calls == [CANDS[2]] and res == ["result"]
     # another key tunes again and keeps the first entry
     fb.calls.clear()
@@ -60,9 +60,9 @@ def test_median_not_a_lucky_run(tmp_path):
     seq = {CANDS[0]: [0.5, 0.05, 0.5, 0.5], CANDS[1]: [0.2, 0.2, 0.2, 0.2], CANDS[2]: [0.3, 0.3, 0.3, 0.3]}
 
     class Seq(FakeBatch):
-        def run(self, w, m, c):
-            self.calls.append((w, m, c))
-            self.now += seq[(w, m, c)].pop(0)
+        def run(self, *cand):
+            self.calls.append(cand)
+            self.now += seq[cand].pop(0)
             return ["r"]
 
     fb = Seq({})
@@ -80,6 +80,14 @@ def test_retune_and_unreadable_cache(tmp_path):
     _, t = SV.autotune(fb.run, "k", str(path), CANDS, retune=True, clock=fb.clock)
     assert (t.workers, t.site_method) == (4, BM_SITES_SPHERES)
     assert json.load(open(path))["k"]["workers"] == 4
+
+
+def test_entry_without_every_setting_is_tuned_again(tmp_path):
+    path = tmp_path / "tuning.json"
+    path.write_text(json.dumps({"k": {"workers": 4, "site_method": 0, "concurrent_phases": True, "batch_ms": 9.0}}))
+    fb = FakeBatch({CANDS[0]: 0.3, CANDS[1]: 0.1, CANDS[2]: 0.2})
+    _, t = SV.autotune(fb.run, "k", str(path), CANDS, clock=fb.clock)
+    assert not t.from_cache and t.setting() == CANDS[1]
 
 
 def test_mix_signature_buckets():

@@ -196,6 +196,26 @@ def test_tbth_tbsp_row_widths(gpu_ctx, shape):
         check_stats(got, ref.thickness, sp.spacing_um)
 
 
+@pytest.mark.parametrize("rows", [32, 64])
+def test_fill_tile_rows(gpu_ctx, rows):
+    """Both fill tile shapes (32 x 32 x 16 and 32 x 64 x 16 voxels) give the
+    reference's maps, on heights that are and are not multiples of 64."""
+    for shape, seed in (((40, 100, 72), 61), ((33, 128, 64), 62)):
+        sp = S.make_specimen(shape, 3.0, 0.2, "cylinder", 0.45 * min(shape[1], shape[2]), 11.0, seed)
+        gpu_ctx.set_fill_tile_rows(rows)
+        try:
+            res = analyze_thickness(sp.bone, sp.roi, sp.spacing_um, ctx=gpu_ctx, return_maps=True)
+        finally:
+            gpu_ctx.set_fill_tile_rows(0)
+        for sel, got, gmap in ((True, res.thickness, res.thickness_map), (False, res.spacing, res.spacing_map)):
+            m = O.phase_inside(sp.bone, sp.roi, sel)
+            ref = O.local_thickness(m, O.FOREGROUND)
+            assert np.array_equal(gmap.view(np.uint32), ref.thickness.view(np.uint32))
+            check_stats(got, ref.thickness, sp.spacing_um)
+    with pytest.raises(BoneMorphometryError, match="fill tile rows must be"):
+        gpu_ctx.set_fill_tile_rows(48)
+
+
 def test_device_tensor_path(gpu_ctx):
     import torch
 

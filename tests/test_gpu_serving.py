@@ -46,8 +46,9 @@ def test_batch_device_pointers_and_quantiles(gpu_ctx):
 
 def test_tuned_batch_equals_alone(gpu_ctx, tmp_path):
     """The tuner runs the batch under each candidate (worker count, site
-    method, phase scheduling): the results equal the specimens' results alone,
-    and the second call reads its settings from the cache."""
+    method, fill tile rows, phase scheduling): the results equal the
+    specimens' results alone, and the second call reads its settings from the
+    cache."""
     from bone_morphometry_gb300 import Context
     from bone_morphometry_gb300._lib import BM_SITES_AUTO, BM_SITES_CHAINS, BM_SITES_SPHERES
     from bone_morphometry_gb300.serving import tuned_batch_tbth_tbsp
@@ -55,12 +56,12 @@ def test_tuned_batch_equals_alone(gpu_ctx, tmp_path):
     items = small_specimens(6, seed=5)
     alone = [analyze_thickness(s.bone, s.roi, s.spacing_um, ctx=gpu_ctx) for s in items]
     inputs = [SpecimenInput(s.bone, s.roi, s.spacing_um) for s in items]
-    cands = ((2, BM_SITES_AUTO, True), (3, BM_SITES_SPHERES, False), (2, BM_SITES_CHAINS, True))
+    cands = ((2, BM_SITES_AUTO, 32, True), (3, BM_SITES_SPHERES, 64, False), (2, BM_SITES_CHAINS, 64, True))
     path = str(tmp_path / "tuning.json")
     ctx = Context()
     try:
         res, t = tuned_batch_tbth_tbsp(inputs, ctx=ctx, cache_path=path, candidates=cands)
-        assert not t.from_cache and (t.workers, t.site_method, t.concurrent_phases) in cands
+        assert not t.from_cache and t.setting() in cands
         for a, (th, sp, st) in zip(alone, res):
             assert st == 0 and same(a.thickness, th) and same(a.spacing, sp)
         res2, t2 = tuned_batch_tbth_tbsp(inputs, ctx=ctx, cache_path=path, candidates=cands)
