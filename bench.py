@@ -95,6 +95,8 @@ def parse_args(argv=None):
     ap.add_argument("--profile-case", type=int, default=0, metavar="N",
                     help="run the profiling case at edge N instead of the benchmark")
     ap.add_argument("--plates", action="store_true", help="profiling case with the 1024^3 plate generator")
+    ap.add_argument("--fill-rows", type=int, default=0, choices=(0, 32, 64),
+                    help="profiling case: the fill's tile rows (0: 64, as on the 512^3 and 1024^3 workloads)")
     return ap.parse_args(argv)
 
 
@@ -674,6 +676,8 @@ def run_profile_case(args) -> int:
         sp = S.make_specimen((n, n, n), 5.0, 0.15, "cylinder", 0.47 * n, 19.5, 1002)
     ctx = Context(0)
     ctx.set_concurrent_phases(False)
+    # the fill tile shape of the 512^3 and 1024^3 workloads (a 384^3 case alone would get 32-row tiles)
+    ctx.set_fill_tile_rows(64 if args.fill_rows == 0 else args.fill_rows)
     bone = torch.from_numpy(sp.bone).cuda()
     roi = torch.from_numpy(sp.roi).cuda()
     for _ in range(2):
