@@ -226,7 +226,7 @@ class Context:
         self.call("bm_ctx_set_site_method", int(method))
 
     def set_fill_tile_rows(self, rows: int = 0) -> None:
-        """Rows of y in the sphere fill's tiles: 0 (by volume size), 32 or 64."""
+        """Rows of y in the sphere fill's tiles: 0 (by volume size), 16, 32 or 64."""
         self.call("bm_ctx_set_fill_tile_rows", int(rows))
 
     def set_wait_cycles(self, cycles: int = -1) -> None:

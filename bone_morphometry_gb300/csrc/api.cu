@@ -1096,8 +1096,8 @@ int bm_ctx_set_site_method(bm_ctx* ctx, int method) {
 
 int bm_ctx_set_fill_tile_rows(bm_ctx* ctx, int rows) {
   return guarded(ctx, [&]() -> int {
-    if (rows != 0 && rows != 32 && rows != 64)
-      fail(ctx, BM_ERR_INVALID, "fill tile rows must be 0 (by volume size), 32 or 64; got %d", rows);
+    if (rows != 0 && rows != 16 && rows != 32 && rows != 64)
+      fail(ctx, BM_ERR_INVALID, "fill tile rows must be 0 (by volume size), 16, 32 or 64; got %d", rows);
     ctx->fill_rows = rows;
     if (ctx->twin) ctx->twin->fill_rows = rows;
     return BM_OK;

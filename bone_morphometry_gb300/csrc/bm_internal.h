@@ -117,13 +117,15 @@ struct FixedPartial {
   unsigned long long pad;
 };
 
-// Tile of the tile-owned sphere fill: 32 x (32 or 64) x 16 voxels (x, y, z).
+// Tile of the tile-owned sphere fill: 32 x (16, 32 or 64) x 16 voxels (x, y, z).
 constexpr int kFillTX = 32;
 constexpr int kFillTZ = 16;
-// Volumes of at least this many voxels fill 64-row tiles by default, smaller
-// ones 32-row tiles (measured: 512^3 5.1 against 5.6 ms per launch with 64
-// rows; 128^3 0.35 against 0.55 ms with 32).
+// Volumes of at least kFillTallMinVoxels fill 64-row tiles by default, those
+// of at least kFillMidMinVoxels 32-row tiles, smaller ones 16-row tiles
+// (measured: 512^3 5.1 against 5.6 ms per launch with 64 rows; 128^3 0.26
+// ms with 16 rows, 0.36 with 32, 0.55 with 64).
 constexpr long long kFillTallMinVoxels = 1ll << 26;
+constexpr long long kFillMidMinVoxels = 1ll << 22;
 
 // Largest r^2 whose sphere lattice points the tile fill tabulates (radius 256);
 // volumes with larger distances use the per-ball atomic fill.
@@ -192,7 +194,7 @@ struct bm_ctx {
   bm_ctx* twin = nullptr;
   cudaEvent_t inputs_ready = nullptr;
   bool split_phases = true;  // false: both phases on this context, one after the other
-  int fill_rows = 0;         // rows of y per fill tile: 0 = by volume size, or 32 / 64
+  int fill_rows = 0;         // rows of y per fill tile: 0 = by volume size, or 16 / 32 / 64
   int site_method = 0;       // BM_SITES_*
   long long wait_cycles = -1;  // first-wait limit of the bounded device waits (< 0: default)
   std::mutex mu;

@@ -5,8 +5,8 @@
 // every voxel is covered ~500 times).  Here the work splits in two:
 //
 // Selected voxels: the output volume is cut into 32x64x16 tiles (32x32x16 for
-// volumes below 2^26 voxels), each owned by one CTA that paints its tile in
-// shared memory.  The balls that reach a tile
+// volumes below 2^26 voxels, 32x16x16 below 2^22), each owned by one CTA that
+// paints its tile in shared memory.  The balls that reach a tile
 // are visited in strictly descending r^2 (a counting sort by (tile, r^2
 // rank)); the final value of a voxel is the r^2 of the first -- largest --
 // ball that covers it, so per-row bitmasks of still-unpainted voxels let every
@@ -204,16 +204,16 @@ constexpr int kRotLevels = 6;     // range-OR levels: spans 1, 2, 4, 8, 16, 32 r
                                   // two 32-row lookups cover a plane's 64 rows
 constexpr int kRotEvery = 4;      // non-empty bins between rebuilds of the range-OR table
 
-// The tile shape: 32 x TY x 16 voxels, TY = 32 or 64 rows of y.  Taller tiles
-// give fewer ball entries and plane tests per voxel, shorter ones more tiles
-// (a small volume's fill is bound by its tiles' serial chains of r^2 bins).
+// The tile shape: 32 x TY x 16 voxels, TY = 16, 32 or 64 rows of y.  Taller
+// tiles give fewer ball entries and plane tests per voxel, shorter ones more
+// tiles (a small volume's fill is bound by its tiles' serial chains of r^2 bins).
 template <int TY>
 struct FillTile {
-  static_assert(TY == 32 || TY == 64, "32 or 64 rows per tile");
+  static_assert(TY == 16 || TY == 32 || TY == 64, "16, 32 or 64 rows per tile");
   static constexpr int kRows = kFillTZ * TY;
   static constexpr int kRotStride = TY + 1;  // words per range-OR row: lanes on different planes hit different banks
   // (ball, plane) paint items per round: as many as 5 CTAs per SM leave room for
-  static constexpr int kItems = TY == 32 ? 4096 : 2048;
+  static constexpr int kItems = TY == 64 ? 2048 : 4096;
   static constexpr int kRound = kItems / kFillTZ;  // balls tested per round (each yields at most kFillTZ items)
   static constexpr size_t kSmemWords = (size_t)kRows + kRows + (kBinChunk + 4) + kBinChunk + kEntWin +
                                        (kRotLevels - 1) * kFillTZ * kRotStride + kItems + 130;
@@ -224,7 +224,7 @@ static_assert(kEntWin <= (1 << 16) && kFillTZ <= 16, "paint item encoding (and r
 // rot[lv - 1][z][y] (rows of TY + 1 words) = OR of the unpainted-voxel masks
 // of rows y .. y + 2^lv - 1 of plane z (rows past the tile edge count as
 // empty), lv = 1 .. 5.  Built with shuffles, one plane per warp step; lane l
-// holds row l (and l + 32 in 64-row tiles).
+// holds row l (and l + 32 in 64-row tiles; lanes past a 16-row tile hold nothing).
 template <int TY>
 __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uint32_t* __restrict__ rot, int warp,
                                           int lane, int nwarps) {
@@ -245,12 +245,12 @@ __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uin
         rr[lane + 32] = v1;
       }
     } else {
-      uint32_t v = usel[urow<TY>(zz, lane)];
+      uint32_t v = lane < TY ? usel[urow<TY>(zz, lane)] : 0u;
 #pragma unroll
       for (int lv = 1; lv < kRotLevels; ++lv) {
         const uint32_t u = __shfl_down_sync(0xffffffffu, v, 1 << (lv - 1));
         v |= (lane + (1 << (lv - 1)) < 32) ? u : 0u;
-        rot[((lv - 1) * kFillTZ + zz) * kStride + lane] = v;
+        if (lane < TY) rot[((lv - 1) * kFillTZ + zz) * kStride + lane] = v;
       }
     }
   }
@@ -260,8 +260,8 @@ __device__ __forceinline__ void build_rot(const uint32_t* __restrict__ usel, uin
 // A painted voxel's r^2 goes straight to the map (each selected voxel is
 // painted once: its bit in usel is cleared atomically first), and the voxels
 // left unpainted get 0 at the end; without a per-voxel value array the CTA
-// needs 37 KB (32 rows) or 44 KB (64 rows) of shared memory, and 5 CTAs share
-// an SM (48 registers).
+// needs 30 KB (16 rows), 37 KB (32 rows) or 44 KB (64 rows) of shared memory,
+// and 5 CTAs share an SM (48 registers).
 // Shared memory:
 //   sown : per row (z, y), the tile's selected voxels;
 //   usel : per row (z, y), the selected voxels not yet painted;
@@ -628,8 +628,8 @@ inline unsigned blocks_for(long long work, int per_block, long long cap) {
 }  // namespace
 
 int fill_tile_rows(Dims dm, int requested) {
-  if (requested == 32 || requested == 64) return requested;
-  return dm.n() >= kFillTallMinVoxels ? 64 : 32;
+  if (requested == 16 || requested == 32 || requested == 64) return requested;
+  return dm.n() >= kFillTallMinVoxels ? 64 : dm.n() >= kFillMidMinVoxels ? 32 : 16;
 }
 
 long long fill_tile_count(Dims dm, int ty) { return geom_of(dm, ty).ntiles; }
@@ -777,8 +777,9 @@ cudaError_t launch_tile_fill(const uint32_t* entries, const uint32_t* offsets, c
   tile_weight_hist_kernel<<<ob, 256, 0, s>>>(offsets, info, g.ntiles, hist);
   tile_weight_scan_kernel<<<1, 1, 0, s>>>(hist);
   tile_weight_scatter_kernel<<<ob, 256, 0, s>>>(offsets, info, g.ntiles, hist, order);
-  e = ty == 64 ? launch_tile_fill_rows<64>(entries, offsets, rvals, rgeo, info, selbits, dm, g, order, fillmap, s)
-              : launch_tile_fill_rows<32>(entries, offsets, rvals, rgeo, info, selbits, dm, g, order, fillmap, s);
+  e = ty == 64   ? launch_tile_fill_rows<64>(entries, offsets, rvals, rgeo, info, selbits, dm, g, order, fillmap, s)
+      : ty == 32 ? launch_tile_fill_rows<32>(entries, offsets, rvals, rgeo, info, selbits, dm, g, order, fillmap, s)
+                 : launch_tile_fill_rows<16>(entries, offsets, rvals, rgeo, info, selbits, dm, g, order, fillmap, s);
   *launches += 4;
   if (e != cudaSuccess) return e;
   return cudaGetLastError();

@@ -89,8 +89,9 @@ cudaError_t launch_dia_table(const uint4* lut, uint32_t n, float* dia, cudaStrea
 
 // Tile-owned fill (fill.cu).
 // Rows of y per fill tile: 64 for volumes of at least kFillTallMinVoxels (fewer
-// ball entries per voxel), else 32 (more tiles: a small volume's fill is bound
-// by its tiles' serial chains); requested = 32 or 64 forces it.
+// ball entries per voxel), 32 from kFillMidMinVoxels, else 16 (more tiles: a
+// small volume's fill is bound by its tiles' serial chains); requested = 16,
+// 32 or 64 forces it.
 int fill_tile_rows(Dims dm, int requested);
 long long fill_tile_count(Dims dm, int ty);
 size_t scan_scratch_words(long long n);

@@ -77,14 +77,15 @@ def batch_tbth_tbsp(specimens, feature_mode=FeatureMode.CLASSIC, ctx: Context | 
 # number of workers, how the fill finds the non-selected voxels that ridge
 # spheres reach (the sphere lattice points, a scatter per ridge, or the chain
 # passes, a gather along the distance transform's argmins; local_thickness.rs:169-202
-# paints them too), the fill's tile shape (32 x 32 x 16 or 32 x 64 x 16 voxels),
+# paints them too), the fill's tile shape (by each specimen's size, or 32 x 32 x 16
+# or 32 x 64 x 16 voxels for all),
 # and whether each specimen's two phases run side by side.  The tuner runs the
 # whole batch for every candidate and keeps the fastest, per GPU and per mix of
 # specimen sizes, in a JSON file, so a later batch of the same kind starts from
 # the stored choice.
 
-TUNE_CANDIDATES = tuple((w, m, r, c) for w in (4, 6, 8) for m in (BM_SITES_AUTO, BM_SITES_SPHERES, BM_SITES_CHAINS)
-                        for r in (32, 64) for c in (True, False))
+TUNE_CANDIDATES = tuple((w, m, r, c) for w in (6, 8) for m in (BM_SITES_AUTO, BM_SITES_SPHERES, BM_SITES_CHAINS)
+                        for r in (0, 32, 64) for c in (True, False))
 _TUNE_FIELDS = ("workers", "site_method", "fill_tile_rows", "concurrent_phases")
 
 
