@@ -121,11 +121,12 @@ struct FixedPartial {
 constexpr int kFillTX = 32;
 constexpr int kFillTZ = 16;
 // Volumes of at least kFillTallMinVoxels fill 64-row tiles by default, those
-// of at least kFillMidMinVoxels 32-row tiles, smaller ones 16-row tiles
-// (measured: 512^3 5.1 against 5.6 ms per launch with 64 rows; 128^3 0.26
-// ms with 16 rows, 0.36 with 32, 0.55 with 64).
-constexpr long long kFillTallMinVoxels = 1ll << 26;
-constexpr long long kFillMidMinVoxels = 1ll << 22;
+// of at least kFillMidMinVoxels 32-row tiles, smaller ones 16-row tiles.
+// Measured on the 512^3 generator's specimens at other edges (ms per fill
+// launch, 16 / 32 / 64 rows): 192^3 0.65 / 0.85 / 1.36, 256^3 1.06 / 1.08 /
+// 1.51, 320^3 1.83 / 1.57 / 1.66, 384^3 3.15 / 2.65 / 2.40, 512^3 - / 5.6 / 5.1.
+constexpr long long kFillTallMinVoxels = 3ll << 24;
+constexpr long long kFillMidMinVoxels = 1ll << 24;
 
 // Largest r^2 whose sphere lattice points the tile fill tabulates (radius 256);
 // volumes with larger distances use the per-ball atomic fill.

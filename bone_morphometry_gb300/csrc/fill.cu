@@ -5,8 +5,8 @@
 // every voxel is covered ~500 times).  Here the work splits in two:
 //
 // Selected voxels: the output volume is cut into 32x64x16 tiles (32x32x16 for
-// volumes below 2^26 voxels, 32x16x16 below 2^22), each owned by one CTA that
-// paints its tile in shared memory.  The balls that reach a tile
+// volumes below 3 * 2^24 voxels, 32x16x16 below 2^24), each owned by one CTA
+// that paints its tile in shared memory.  The balls that reach a tile
 // are visited in strictly descending r^2 (a counting sort by (tile, r^2
 // rank)); the final value of a voxel is the r^2 of the first -- largest --
 // ball that covers it, so per-row bitmasks of still-unpainted voxels let every

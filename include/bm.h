@@ -296,10 +296,10 @@ enum { BM_SITES_AUTO = 0, BM_SITES_SPHERES = 1, BM_SITES_CHAINS = 2 };
 int bm_ctx_set_site_method(bm_ctx* ctx, int method);
 
 /* Rows of y in the sphere fill's tiles (32 x rows x 16 voxels): 0 (the
- * default) picks 64 for volumes of at least 2^26 voxels (fewer ball entries
- * and plane tests per voxel), 32 from 2^22 voxels and 16 below (more tiles,
- * shorter serial chains); 16, 32 or 64 forces it.  Results are identical
- * either way. */
+ * default) picks 64 for volumes of at least 3 * 2^24 voxels (fewer ball
+ * entries and plane tests per voxel), 32 from 2^24 voxels and 16 below (more
+ * tiles, shorter serial chains); 16, 32 or 64 forces it.  Results are
+ * identical either way. */
 int bm_ctx_set_fill_tile_rows(bm_ctx* ctx, int rows);
 
 /* Cycle limit of the device-side bounded waits of this context's kernels (the
