@@ -153,6 +153,9 @@ def autotune(run, key: str, path: str, candidates=TUNE_CANDIDATES, retune: bool 
     then `repeats` times timed; the candidate with the lowest median time is
     stored under key (single batch times vary by ~15% from run to run).  On a
     hit only the stored candidate runs.  Returns (results, Tuning)."""
+    candidates = tuple(candidates)
+    if not candidates:
+        raise ValueError("autotune needs at least one candidate setting")
     cache = _load_cache(path)
     hit = cache.get(key)
     if hit is not None and all(f in hit for f in _TUNE_FIELDS) and not retune:

@@ -90,6 +90,13 @@ def test_entry_without_every_setting_is_tuned_again(tmp_path):
     assert not t.from_cache and t.setting() == CANDS[1]
 
 
+def test_no_candidates(tmp_path):
+    import pytest
+
+    with pytest.raises(ValueError, match="at least one candidate"):
+        SV.autotune(lambda *c: None, "k", str(tmp_path / "t.json"), ())
+
+
 def test_mix_signature_buckets():
     a = SV.mix_signature([(96, 100, 120), (384, 300, 200)])
     b = SV.mix_signature([(200, 300, 384), (120, 100, 96)])  # order and axis order do not matter
